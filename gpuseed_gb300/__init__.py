@@ -1,0 +1,235 @@
+"""gpuseed_gb300 -- GB300-native seeding (MEM/SMEM by FM-index backward search).
+
+Python front end of libgpuseed.so, mirroring the reference's seed_gen interface
+(nahmedraja/GPUseed seed_gen.cu:2817-3815): an index loaded from the .bwt/.sa
+files, a batch of reads, the -k/-s switches, and seeds in the reference's
+output order and text format.  All compute runs in the CUDA library; importing
+this module fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libgpuseed.so")
+CLI_PATH = os.path.join(_PKG, "seed_gen")
+
+N_WILDCARD, N_STOP = 0, 1
+LF_GPUSEED, LF_BWA = 0, 1
+KERNEL_BATCHED, KERNEL_PLAIN = 0, 1
+
+GS_ERRORS = {-1: "EINVAL", -2: "EIO", -3: "EFORMAT", -4: "ENOMEM", -5: "ECUDA", -6: "EWALK",
+             -7: "EOVERFLOW", -8: "ETIMEOUT", -9: "ESTATE"}
+
+# Every symbol include/gpuseed.h declares.
+EXPORTS = ["gs_index_load", "gs_index_from_host", "gs_index_free", "gs_index_get_info",
+           "gs_index_kmer_table", "gs_index_set_l2_window", "gs_ctx_create", "gs_ctx_free",
+           "gs_seed", "gs_seed_device", "gs_result_host", "gs_result_device",
+           "gs_result_write_text", "gs_ctx_stream", "gs_ctx_last_timing", "gs_last_error",
+           "gs_strerror", "gs_version"]
+
+
+class GsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{GS_ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [("k", C.c_int32), ("smem", C.c_int32), ("n_mode", C.c_int32),
+                ("lf_mode", C.c_int32), ("kernel", C.c_int32), ("queue_chunk", C.c_int32),
+                ("ctas_per_sm", C.c_int32), ("reserved", C.c_int32)]
+
+
+class SeedRec(C.Structure):
+    _fields_ = [("x", C.c_int32), ("y", C.c_int32), ("l", C.c_uint32), ("u", C.c_uint32),
+                ("xl", C.c_uint32), ("xu", C.c_uint32), ("n_pos", C.c_uint32),
+                ("pad", C.c_uint32)]
+
+
+class ResultView(C.Structure):
+    _fields_ = [("n_reads", C.c_uint32), ("n_seeds", C.c_uint64), ("n_pos", C.c_uint64),
+                ("read_seed_off", C.POINTER(C.c_uint64)), ("read_pos_off", C.POINTER(C.c_uint64)),
+                ("seeds", C.POINTER(SeedRec)), ("pos", C.POINTER(C.c_uint32))]
+
+
+class IndexInfo(C.Structure):
+    _fields_ = [("seq_len", C.c_uint32), ("primary", C.c_uint32), ("sa_intv", C.c_uint32),
+                ("n_sa", C.c_uint32), ("L2", C.c_uint32 * 5), ("device", C.c_int32),
+                ("device_bytes", C.c_uint64)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libgpuseed.so; raises if it was not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() "
+                              "(nvcc for sm_103a); there is no CPU fallback")
+        L = C.CDLL(LIB_PATH)
+        vp, u32, u64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
+        L.gs_index_load.argtypes = [C.c_char_p, i32, C.POINTER(vp)]
+        L.gs_index_from_host.argtypes = [u32, vp, vp, u64, u32, vp, u64, i32, C.POINTER(vp)]
+        L.gs_index_free.argtypes = [vp]
+        L.gs_index_get_info.argtypes = [vp, C.POINTER(IndexInfo)]
+        L.gs_index_kmer_table.argtypes = [vp, u64, u64, vp]
+        L.gs_index_set_l2_window.argtypes = [vp, C.c_float]
+        L.gs_ctx_create.argtypes = [vp, vp, C.POINTER(vp)]
+        L.gs_ctx_free.argtypes = [vp]
+        L.gs_seed.argtypes = [vp, vp, vp, vp, u32, C.POINTER(Params)]
+        L.gs_seed_device.argtypes = [vp, vp, vp, vp, u32, C.POINTER(Params), i32]
+        L.gs_result_host.argtypes = [vp, C.POINTER(ResultView)]
+        L.gs_result_device.argtypes = [vp, C.POINTER(ResultView)]
+        L.gs_result_write_text.argtypes = [vp, i32, u32, i32]
+        L.gs_ctx_stream.argtypes = [vp]
+        L.gs_ctx_stream.restype = vp
+        L.gs_ctx_last_timing.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.gs_last_error.restype = C.c_char_p
+        L.gs_strerror.restype = C.c_char_p
+        L.gs_strerror.argtypes = [i32]
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != 0:
+        raise GsError(rc, lib().gs_last_error().decode(errors="replace"))
+    return rc
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class Index:
+    """Device-resident index (.bwt + .sa + 13-mer table)."""
+
+    def __init__(self, prefix: str | None = None, device: int = 0, *, arrays=None):
+        h = C.c_void_p()
+        if arrays is not None:
+            primary, L2_1to4, bwt, sa_samples, sa_intv = arrays
+            L2a = np.ascontiguousarray(L2_1to4, dtype=np.uint32)
+            bwt = np.ascontiguousarray(bwt, dtype=np.uint32)
+            sa_samples = np.ascontiguousarray(sa_samples, dtype=np.uint32)
+            check(lib().gs_index_from_host(primary, _ptr(L2a), _ptr(bwt), bwt.size, sa_intv,
+                                           _ptr(sa_samples), sa_samples.size, device, C.byref(h)))
+        else:
+            check(lib().gs_index_load(prefix.encode(), device, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gs_index_free(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def info(self) -> IndexInfo:
+        inf = IndexInfo()
+        check(lib().gs_index_get_info(self.h, C.byref(inf)))
+        return inf
+
+    def kmer_table(self, first=0, count=None) -> np.ndarray:
+        if count is None:
+            count = (1 << 26) - first
+        out = np.empty(2 * count, dtype=np.uint32)
+        check(lib().gs_index_kmer_table(self.h, first, count, _ptr(out)))
+        return out
+
+    def set_l2_window(self, hit_ratio: float):
+        check(lib().gs_index_set_l2_window(self.h, hit_ratio))
+
+
+class Result:
+    """Host copy of one batch's seeds in output order."""
+
+    def __init__(self, view: ResultView):
+        n = view.n_reads
+        self.n_reads = n
+        self.read_seed_off = np.ctypeslib.as_array(view.read_seed_off, (n + 1,)).copy()
+        self.read_pos_off = np.ctypeslib.as_array(view.read_pos_off, (n + 1,)).copy()
+        ns, npos = int(view.n_seeds), int(view.n_pos)
+        if ns:
+            raw = np.ctypeslib.as_array(C.cast(view.seeds, C.POINTER(C.c_uint32)), (ns * 8,))
+            self.seeds = raw.reshape(ns, 8).copy()  # x y l u xl xu n_pos pad
+        else:
+            self.seeds = np.zeros((0, 8), np.uint32)
+        self.pos = np.ctypeslib.as_array(view.pos, (npos,)).copy() if npos else np.zeros(0, np.uint32)
+
+    def read_records(self, r):
+        """[(x, y, l, u, [positions...]), ...] of read r in output order."""
+        out = []
+        p = int(self.read_pos_off[r])
+        for s in range(int(self.read_seed_off[r]), int(self.read_seed_off[r + 1])):
+            x, y, l, u, xl, xu, n, _ = (int(v) for v in self.seeds[s])
+            out.append((x, y, l, u, self.pos[p:p + n].tolist()))
+            p += n
+        return out
+
+
+class Context:
+    """One stream + workspace; seeds batches of reads."""
+
+    def __init__(self, index: Index, stream=None):
+        self.index = index
+        h = C.c_void_p()
+        check(lib().gs_ctx_create(index.h, C.c_void_p(stream) if stream else None, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gs_ctx_free(self.h)
+            self.h = None
+
+    __del__ = close
+
+    @staticmethod
+    def params(k=20, smem=False, n_mode=N_WILDCARD, lf_mode=LF_GPUSEED, kernel=KERNEL_BATCHED,
+               queue_chunk=0, ctas_per_sm=0) -> Params:
+        return Params(k, 1 if smem else 0, n_mode, lf_mode, kernel, queue_chunk, ctas_per_sm, 0)
+
+    def seed(self, seqs, offsets, lengths, **kw) -> Result:
+        """Reads in host memory; returns the host result."""
+        buf = np.frombuffer(seqs, dtype=np.uint8) if isinstance(seqs, (bytes, bytearray)) else \
+            np.ascontiguousarray(seqs, dtype=np.uint8)
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+        lengths = np.ascontiguousarray(lengths, dtype=np.uint32)
+        p = self.params(**kw)
+        check(lib().gs_seed(self.h, _ptr(buf), _ptr(offsets), _ptr(lengths), lengths.size,
+                            C.byref(p)))
+        return self.result()
+
+    def seed_device(self, d_seqs: int, d_offsets: int, d_lengths: int, n_reads: int,
+                    fetch=False, **kw):
+        """Reads already in device memory (raw device pointers)."""
+        p = self.params(**kw)
+        check(lib().gs_seed_device(self.h, C.c_void_p(d_seqs), C.c_void_p(d_offsets),
+                                   C.c_void_p(d_lengths), n_reads, C.byref(p), 1 if fetch else 0))
+        return self.result() if fetch else None
+
+    def result(self) -> Result:
+        v = ResultView()
+        check(lib().gs_result_host(self.h, C.byref(v)))
+        return Result(v)
+
+    def device_counts(self):
+        v = ResultView()
+        check(lib().gs_result_device(self.h, C.byref(v)))
+        return int(v.n_seeds), int(v.n_pos)
+
+    def write_text(self, fd: int, first_read_no: int = 1, smem: bool = False):
+        check(lib().gs_result_write_text(self.h, fd, first_read_no, 1 if smem else 0))
+
+    def stream(self) -> int:
+        return lib().gs_ctx_stream(self.h) or 0
+
+    def last_timing(self):
+        a, b = C.c_float(), C.c_float()
+        check(lib().gs_ctx_last_timing(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value

@@ -1,0 +1,570 @@
+/*
+ * gs_api.cu -- seeding context: workspace, the per-batch pipeline, results,
+ * text records and error reporting.
+ *
+ * One gs_seed* call does for one batch what the body of seed_gen's batch loop
+ * does (seed_gen.cu:2910-3790), on one stream, with the workspace kept across
+ * calls instead of ~15 cudaMalloc/cudaFree per batch (:3029-3102,
+ * :3750-3770):
+ *
+ *   prepare  -> slot / work-item counts per read, exclusive scans
+ *   search   -> one record slot per candidate (gs_search.cu)
+ *   count    -> per-read compaction + filter counts (gs_post.cu)
+ *   scan     -> seed / position offsets
+ *   emit     -> output seeds in output order
+ *   locate   -> positions by the sampled-SA walk
+ */
+#include "gs_internal.h"
+
+#include <cub/cub.cuh>
+
+#include <errno.h>
+#include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+/* ------------------------------------------------------------------ */
+/* errors */
+
+static thread_local char g_err[512];
+
+void gs_set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int gs_cuda_fail(cudaError_t e, const char *what)
+{
+    gs_set_error("%s: %s", what, cudaGetErrorString(e));
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return GS_ENOMEM;
+    }
+    return GS_ECUDA;
+}
+
+extern "C" const char *gs_last_error(void) { return g_err; }
+
+extern "C" const char *gs_strerror(int code)
+{
+    switch (code) {
+    case GS_OK: return "ok";
+    case GS_EINVAL: return "invalid argument";
+    case GS_EIO: return "i/o error";
+    case GS_EFORMAT: return "index format error";
+    case GS_ENOMEM: return "out of memory";
+    case GS_ECUDA: return "CUDA error";
+    case GS_EWALK: return "sampled-SA walk exceeded its limit";
+    case GS_EOVERFLOW: return "output capacity exceeded";
+    case GS_ETIMEOUT: return "bounded wait ran out";
+    case GS_ESTATE: return "invalid state";
+    default: return "unknown error";
+    }
+}
+
+extern "C" int gs_version(void) { return 100; }
+
+/* ------------------------------------------------------------------ */
+/* index accessors (gs_index.cu) */
+
+const GsDevIndex *gs_index_dev(const gs_index *idx);
+int gs_index_device(const gs_index *idx);
+float gs_index_l2_ratio(const gs_index *idx);
+size_t gs_index_occ_bytes(const gs_index *idx);
+
+/* ------------------------------------------------------------------ */
+/* context */
+
+template <class T>
+static int grow(T *&p, size_t &cap, size_t n)
+{
+    if (n <= cap && p) return GS_OK;
+    size_t nc = n + n / 4 + 64;
+    T *np = NULL;
+    cudaError_t e = cudaMalloc(&np, nc * sizeof(T));
+    if (e != cudaSuccess) return gs_cuda_fail(e, "cudaMalloc(workspace)");
+    cudaFree(p);
+    p = np;
+    cap = nc;
+    return GS_OK;
+}
+
+template <class T>
+static int grow_host(T *&p, size_t &cap, size_t n)
+{
+    if (n <= cap && p) return GS_OK;
+    size_t nc = n + n / 4 + 64;
+    T *np = NULL;
+    cudaError_t e = cudaMallocHost(&np, nc * sizeof(T));
+    if (e != cudaSuccess) return gs_cuda_fail(e, "cudaMallocHost(result)");
+    cudaFreeHost(p);
+    p = np;
+    cap = nc;
+    return GS_OK;
+}
+
+struct gs_ctx {
+    gs_index *idx;
+    cudaStream_t st;
+    bool own_stream;
+    cudaEvent_t ev0, ev_s0, ev_s1, ev1;
+    /* inputs staged by gs_seed_rec */
+    char *d_seqs; size_t cap_seqs;
+    uint64_t *d_offsets; size_t cap_offsets;
+    uint32_t *d_lengths; size_t cap_lengths;
+    /* per read */
+    uint64_t *slot_cnt, *slot_off; size_t cap_slot_cnt, cap_slot_off;
+    uint32_t *item_cnt, *item_off; size_t cap_item_cnt, cap_item_off;
+    uint32_t *rd_nf, *rd_nr; size_t cap_nf, cap_nr;
+    uint64_t *rd_nseeds, *rd_npos; size_t cap_rns, cap_rnp;
+    uint64_t *seed_off, *pos_off; size_t cap_so, cap_po;
+    /* per candidate / base / output */
+    GsRec *slots; size_t cap_slots;
+    uint32_t *hist; size_t cap_hist;
+    gs_seed_rec *seeds; size_t cap_seeds;
+    uint64_t *seed_pos; size_t cap_seed_pos;
+    uint32_t *pos; size_t cap_pos;
+    uint32_t *pmap; size_t cap_pmap;
+    uint32_t *queue;
+    uint64_t *d_max;
+    void *cub_tmp; size_t cap_cub;
+    uint64_t *h_small;          /* pinned scalars */
+    /* host result */
+    uint64_t *h_seed_off; size_t cap_h_so;
+    uint64_t *h_pos_off; size_t cap_h_po;
+    gs_seed_rec *h_seeds; size_t cap_h_seeds;
+    uint32_t *h_pos; size_t cap_h_pos;
+    uint32_t n_reads;
+    uint64_t n_seeds, n_pos;
+    int have_host, have_dev;
+    float t_search, t_total;
+};
+
+extern "C" int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out)
+{
+    if (!idx || !out) return GS_EINVAL;
+    *out = NULL;
+    GS_CUDA(cudaSetDevice(gs_index_device(idx)));
+    gs_ctx *c = (gs_ctx *)calloc(1, sizeof(gs_ctx));
+    if (!c) return GS_ENOMEM;
+    c->idx = idx;
+    cudaError_t e = cudaSuccess;
+    if (cuda_stream) {
+        c->st = (cudaStream_t)cuda_stream;
+    } else {
+        e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+        c->own_stream = true;
+    }
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev_s0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev_s1);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e == cudaSuccess) e = cudaMalloc(&c->queue, 16);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_max, 16);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_small, 64);
+    if (e != cudaSuccess) {
+        int rc = gs_cuda_fail(e, "gs_ctx_create");
+        gs_ctx_free(c);
+        return rc;
+    }
+    float ratio = gs_index_l2_ratio(idx);
+    if (ratio > 0.f) {
+        int dev = gs_index_device(idx), maxwin = 0, persist = 0;
+        cudaDeviceGetAttribute(&maxwin, cudaDevAttrMaxAccessPolicyWindowSize, dev);
+        cudaDeviceGetAttribute(&persist, cudaDevAttrMaxPersistingL2CacheSize, dev);
+        if (maxwin > 0 && persist > 0) {
+            size_t occ = gs_index_occ_bytes(idx);
+            size_t win = occ < (size_t)maxwin ? occ : (size_t)maxwin;
+            cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, (size_t)persist);
+            cudaStreamAttrValue v;
+            memset(&v, 0, sizeof(v));
+            v.accessPolicyWindow.base_ptr = (void *)gs_index_dev(idx)->occ;
+            v.accessPolicyWindow.num_bytes = win;
+            v.accessPolicyWindow.hitRatio = ratio;
+            v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+            v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+            cudaStreamSetAttribute(c->st, cudaStreamAttributeAccessPolicyWindow, &v);
+            cudaGetLastError();
+        }
+    }
+    *out = c;
+    return GS_OK;
+}
+
+extern "C" void gs_ctx_free(gs_ctx *c)
+{
+    if (!c) return;
+    if (c->st) cudaStreamSynchronize(c->st);
+    cudaFree(c->d_seqs); cudaFree(c->d_offsets); cudaFree(c->d_lengths);
+    cudaFree(c->slot_cnt); cudaFree(c->slot_off); cudaFree(c->item_cnt); cudaFree(c->item_off);
+    cudaFree(c->rd_nf); cudaFree(c->rd_nr); cudaFree(c->rd_nseeds); cudaFree(c->rd_npos);
+    cudaFree(c->seed_off); cudaFree(c->pos_off);
+    cudaFree(c->slots); cudaFree(c->hist); cudaFree(c->seeds); cudaFree(c->seed_pos);
+    cudaFree(c->pos); cudaFree(c->pmap); cudaFree(c->queue); cudaFree(c->d_max);
+    cudaFree(c->cub_tmp);
+    cudaFreeHost(c->h_small);
+    cudaFreeHost(c->h_seed_off); cudaFreeHost(c->h_pos_off);
+    cudaFreeHost(c->h_seeds); cudaFreeHost(c->h_pos);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev_s0) cudaEventDestroy(c->ev_s0);
+    if (c->ev_s1) cudaEventDestroy(c->ev_s1);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->own_stream && c->st) cudaStreamDestroy(c->st);
+    free(c);
+}
+
+extern "C" void *gs_ctx_stream(gs_ctx *c) { return c ? (void *)c->st : NULL; }
+
+extern "C" int gs_ctx_last_timing(gs_ctx *c, float *search_ms, float *total_ms)
+{
+    if (!c) return GS_EINVAL;
+    if (search_ms) *search_ms = c->t_search;
+    if (total_ms) *total_ms = c->t_total;
+    return GS_OK;
+}
+
+/* end of the longest read, for the plain kernel's per-base history */
+__global__ void gs_max_end_kernel(const uint64_t *off, const uint32_t *len, uint32_t n,
+                                  unsigned long long *out)
+{
+    uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) atomicMax(out, (unsigned long long)(off[r] + len[r]));
+}
+
+template <class In, class Out>
+static int exclusive_scan(gs_ctx *c, In in, Out out, size_t n)
+{
+    size_t bytes = 0;
+    GS_CUDA(cub::DeviceScan::ExclusiveSum(NULL, bytes, in, out, (int64_t)n, c->st));
+    if (bytes > c->cap_cub) {
+        cudaFree(c->cub_tmp);
+        c->cub_tmp = NULL;
+        c->cap_cub = 0;
+        GS_CUDA(cudaMalloc(&c->cub_tmp, bytes));
+        c->cap_cub = bytes;
+    }
+    GS_CUDA(cub::DeviceScan::ExclusiveSum(c->cub_tmp, bytes, in, out, (int64_t)n, c->st));
+    return GS_OK;
+}
+
+static int check_params(const gs_params *p)
+{
+    if (!p) {
+        gs_set_error("null gs_params");
+        return GS_EINVAL;
+    }
+    if (p->k < GS_K0 || p->k > 1000000) {
+        gs_set_error("min seed length k=%d outside [%d, 1000000]: below 13 the 13-mer lookup "
+                     "would read before the read",
+                     p->k, GS_K0);
+        return GS_EINVAL;
+    }
+    if ((p->n_mode != GS_N_WILDCARD && p->n_mode != GS_N_STOP) ||
+        (p->lf_mode != GS_LF_GPUSEED && p->lf_mode != GS_LF_BWA) ||
+        (p->kernel != GS_KERNEL_BATCHED && p->kernel != GS_KERNEL_PLAIN)) {
+        gs_set_error("gs_params mode out of range");
+        return GS_EINVAL;
+    }
+    return GS_OK;
+}
+
+#define RC(x)                    \
+    do {                         \
+        int _rc = (x);           \
+        if (_rc) return _rc;     \
+    } while (0)
+
+static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets,
+                        const uint32_t *d_lengths, uint32_t n_reads, const gs_params *p,
+                        int fetch)
+{
+    const GsDevIndex &I = *gs_index_dev(c->idx);
+    cudaStream_t st = c->st;
+    c->have_host = c->have_dev = 0;
+    c->n_reads = n_reads;
+    size_t nr1 = (size_t)n_reads + 1;
+    RC(grow(c->slot_cnt, c->cap_slot_cnt, nr1));
+    RC(grow(c->slot_off, c->cap_slot_off, nr1));
+    RC(grow(c->item_cnt, c->cap_item_cnt, nr1));
+    RC(grow(c->item_off, c->cap_item_off, nr1));
+    RC(grow(c->rd_nf, c->cap_nf, nr1));
+    RC(grow(c->rd_nr, c->cap_nr, nr1));
+    RC(grow(c->rd_nseeds, c->cap_rns, nr1));
+    RC(grow(c->rd_npos, c->cap_rnp, nr1));
+    RC(grow(c->seed_off, c->cap_so, nr1));
+    RC(grow(c->pos_off, c->cap_po, nr1));
+
+    GsBatch B;
+    memset(&B, 0, sizeof(B));
+    B.seqs = d_seqs;
+    B.offsets = d_offsets;
+    B.lengths = d_lengths;
+    B.n_reads = n_reads;
+    B.k = p->k;
+    B.smem = p->smem ? 1 : 0;
+    B.n_mode = p->n_mode;
+    B.lf_mode = p->lf_mode;
+    B.queue = c->queue;
+
+    GS_CUDA(cudaEventRecord(c->ev0, st));
+    GS_CUDA(cudaMemsetAsync(c->queue, 0, 16, st));
+    B.slot_off = c->slot_cnt;
+    B.item_off = c->item_cnt;
+    RC(gs_launch_prepare(B, st));
+    RC(exclusive_scan(c, c->slot_cnt, c->slot_off, nr1));
+    RC(exclusive_scan(c, c->item_cnt, c->item_off, nr1));
+    B.slot_off = c->slot_off;
+    B.item_off = c->item_off;
+    GS_CUDA(cudaMemcpyAsync(&c->h_small[0], c->slot_off + n_reads, 8, cudaMemcpyDeviceToHost, st));
+    GS_CUDA(cudaMemcpyAsync(&c->h_small[1], c->item_off + n_reads, 4, cudaMemcpyDeviceToHost, st));
+    if (p->kernel == GS_KERNEL_PLAIN) {
+        GS_CUDA(cudaMemsetAsync(c->d_max, 0, 8, st));
+        if (n_reads)
+            gs_max_end_kernel<<<(n_reads + 255) / 256, 256, 0, st>>>(
+                d_offsets, d_lengths, n_reads, (unsigned long long *)c->d_max);
+        GS_CUDA(cudaMemcpyAsync(&c->h_small[2], c->d_max, 8, cudaMemcpyDeviceToHost, st));
+    }
+    GS_CUDA(cudaStreamSynchronize(st));
+    uint64_t n_slots = c->h_small[0];
+    uint32_t n_items = (uint32_t)(c->h_small[1] & 0xffffffffu);
+    RC(grow(c->slots, c->cap_slots, n_slots + 1));
+    B.slots = c->slots;
+    if (p->kernel == GS_KERNEL_PLAIN) {
+        RC(grow(c->hist, c->cap_hist, c->h_small[2] + 1));
+        B.hist = c->hist;
+    }
+
+    GS_CUDA(cudaEventRecord(c->ev_s0, st));
+    RC(gs_launch_search(I, B, p->kernel, p->queue_chunk, p->ctas_per_sm, n_items, st));
+    GS_CUDA(cudaEventRecord(c->ev_s1, st));
+
+    B.rd_nf = c->rd_nf;
+    B.rd_nr = c->rd_nr;
+    B.rd_nseeds = c->rd_nseeds;
+    B.rd_npos = c->rd_npos;
+    GS_CUDA(cudaMemsetAsync(c->rd_nseeds + n_reads, 0, 8, st));
+    GS_CUDA(cudaMemsetAsync(c->rd_npos + n_reads, 0, 8, st));
+    RC(gs_launch_finalize_count(I, B, st));
+    RC(exclusive_scan(c, c->rd_nseeds, c->seed_off, nr1));
+    RC(exclusive_scan(c, c->rd_npos, c->pos_off, nr1));
+    GS_CUDA(cudaMemcpyAsync(&c->h_small[3], c->seed_off + n_reads, 8, cudaMemcpyDeviceToHost, st));
+    GS_CUDA(cudaMemcpyAsync(&c->h_small[4], c->pos_off + n_reads, 8, cudaMemcpyDeviceToHost, st));
+    GS_CUDA(cudaStreamSynchronize(st));
+    uint64_t n_seeds = c->h_small[3], n_pos = c->h_small[4];
+    if (n_pos > 0xffffffffull * 4) {
+        gs_set_error("batch emits %llu positions; split the batch", (unsigned long long)n_pos);
+        return GS_EOVERFLOW;
+    }
+    RC(grow(c->seeds, c->cap_seeds, n_seeds + 1));
+    RC(grow(c->seed_pos, c->cap_seed_pos, n_seeds + 1));
+    RC(grow(c->pos, c->cap_pos, n_pos + 1));
+    RC(grow(c->pmap, c->cap_pmap, n_pos + 1));
+    B.seed_off = c->seed_off;
+    B.pos_off = c->pos_off;
+    B.seeds = c->seeds;
+    B.seed_pos = c->seed_pos;
+    B.pos = c->pos;
+    B.pmap = c->pmap;
+    B.seed_cap = n_seeds + 1;
+    B.pos_cap = n_pos + 1;
+    RC(gs_launch_finalize_emit(I, B, st));
+    RC(gs_launch_locate(I, B, n_seeds, n_pos, st));
+    GS_CUDA(cudaEventRecord(c->ev1, st));
+    GS_CUDA(cudaMemcpyAsync(&c->h_small[5], c->queue + 1, 4, cudaMemcpyDeviceToHost, st));
+    c->n_seeds = n_seeds;
+    c->n_pos = n_pos;
+    if (fetch) {
+        RC(grow_host(c->h_seed_off, c->cap_h_so, nr1));
+        RC(grow_host(c->h_pos_off, c->cap_h_po, nr1));
+        RC(grow_host(c->h_seeds, c->cap_h_seeds, n_seeds + 1));
+        RC(grow_host(c->h_pos, c->cap_h_pos, n_pos + 1));
+        GS_CUDA(cudaMemcpyAsync(c->h_seed_off, c->seed_off, nr1 * 8, cudaMemcpyDeviceToHost, st));
+        GS_CUDA(cudaMemcpyAsync(c->h_pos_off, c->pos_off, nr1 * 8, cudaMemcpyDeviceToHost, st));
+        if (n_seeds)
+            GS_CUDA(cudaMemcpyAsync(c->h_seeds, c->seeds, n_seeds * sizeof(gs_seed_rec),
+                                    cudaMemcpyDeviceToHost, st));
+        if (n_pos)
+            GS_CUDA(cudaMemcpyAsync(c->h_pos, c->pos, n_pos * 4, cudaMemcpyDeviceToHost, st));
+    }
+    GS_CUDA(cudaStreamSynchronize(st));
+    uint32_t flags = (uint32_t)(c->h_small[5] & 0xffffffffu);
+    cudaEventElapsedTime(&c->t_search, c->ev_s0, c->ev_s1);
+    cudaEventElapsedTime(&c->t_total, c->ev0, c->ev1);
+    if (flags & GS_FLAG_WALK) {
+        gs_set_error("sampled-SA walk exceeded seq_len+2 steps: index inconsistent");
+        return GS_EWALK;
+    }
+    c->have_dev = 1;
+    c->have_host = fetch;
+    return GS_OK;
+}
+
+extern "C" int gs_seed_device(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets,
+                              const uint32_t *d_lengths, uint32_t n_reads, const gs_params *p,
+                              int fetch_to_host)
+{
+    if (!c || (n_reads && (!d_seqs || !d_offsets || !d_lengths))) {
+        gs_set_error("gs_seed_device: null argument");
+        return GS_EINVAL;
+    }
+    RC(check_params(p));
+    GS_CUDA(cudaSetDevice(gs_index_device(c->idx)));
+    return run_pipeline(c, d_seqs, d_offsets, d_lengths, n_reads, p, fetch_to_host);
+}
+
+extern "C" int gs_seed(gs_ctx *c, const char *seqs, const uint64_t *offsets,
+                       const uint32_t *lengths, uint32_t n_reads, const gs_params *p)
+{
+    if (!c || (n_reads && (!seqs || !offsets || !lengths))) {
+        gs_set_error("gs_seed: null argument");
+        return GS_EINVAL;
+    }
+    RC(check_params(p));
+    GS_CUDA(cudaSetDevice(gs_index_device(c->idx)));
+    uint64_t bytes = 0;
+    for (uint32_t r = 0; r < n_reads; r++) {
+        uint64_t e = offsets[r] + lengths[r];
+        if (e > bytes) bytes = e;
+    }
+    RC(grow(c->d_seqs, c->cap_seqs, bytes + 1));
+    RC(grow(c->d_offsets, c->cap_offsets, (size_t)n_reads + 1));
+    RC(grow(c->d_lengths, c->cap_lengths, (size_t)n_reads + 1));
+    if (bytes) GS_CUDA(cudaMemcpyAsync(c->d_seqs, seqs, bytes, cudaMemcpyHostToDevice, c->st));
+    if (n_reads) {
+        GS_CUDA(cudaMemcpyAsync(c->d_offsets, offsets, (size_t)n_reads * 8, cudaMemcpyHostToDevice,
+                                c->st));
+        GS_CUDA(cudaMemcpyAsync(c->d_lengths, lengths, (size_t)n_reads * 4, cudaMemcpyHostToDevice,
+                                c->st));
+    }
+    return run_pipeline(c, c->d_seqs, c->d_offsets, c->d_lengths, n_reads, p, 1);
+}
+
+extern "C" int gs_result_host(gs_ctx *c, gs_result_view *out)
+{
+    if (!c || !out) return GS_EINVAL;
+    if (!c->have_host) {
+        gs_set_error("no host result: last call failed or left it on the device");
+        return GS_ESTATE;
+    }
+    out->n_reads = c->n_reads;
+    out->n_seeds = c->n_seeds;
+    out->n_pos = c->n_pos;
+    out->read_seed_off = c->h_seed_off;
+    out->read_pos_off = c->h_pos_off;
+    out->seeds = c->h_seeds;
+    out->pos = c->h_pos;
+    return GS_OK;
+}
+
+extern "C" int gs_result_device(gs_ctx *c, gs_result_view *out)
+{
+    if (!c || !out) return GS_EINVAL;
+    if (!c->have_dev) {
+        gs_set_error("no device result");
+        return GS_ESTATE;
+    }
+    out->n_reads = c->n_reads;
+    out->n_seeds = c->n_seeds;
+    out->n_pos = c->n_pos;
+    out->read_seed_off = c->seed_off;
+    out->read_pos_off = c->pos_off;
+    out->seeds = c->seeds;
+    out->pos = c->pos;
+    return GS_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* text records (seed_gen.cu:3625-3647) */
+
+struct OutBuf {
+    int fd;
+    char *b;
+    size_t n, cap;
+    int err;
+};
+
+static void ob_flush(OutBuf *o)
+{
+    size_t off = 0;
+    while (off < o->n && !o->err) {
+        ssize_t w = write(o->fd, o->b + off, o->n - off);
+        if (w < 0) {
+            if (errno == EINTR) continue;
+            o->err = 1;
+            break;
+        }
+        off += (size_t)w;
+    }
+    o->n = 0;
+}
+
+static inline void ob_put(OutBuf *o, const char *s, size_t n)
+{
+    if (o->n + n > o->cap) ob_flush(o);
+    memcpy(o->b + o->n, s, n);
+    o->n += n;
+}
+
+static inline void ob_u32(OutBuf *o, uint32_t v)
+{
+    char t[12];
+    int i = 12;
+    do {
+        t[--i] = (char)('0' + v % 10);
+        v /= 10;
+    } while (v);
+    ob_put(o, t + i, (size_t)(12 - i));
+}
+
+extern "C" int gs_result_write_text(gs_ctx *c, int fd, uint32_t first_read_no, int smem)
+{
+    if (!c) return GS_EINVAL;
+    if (!c->have_host) {
+        gs_set_error("no host result to print");
+        return GS_ESTATE;
+    }
+    OutBuf o = {fd, (char *)malloc(1 << 20), 0, 1 << 20, 0};
+    if (!o.b) return GS_ENOMEM;
+    static const char h0[] = "/*===================================";
+    static const char h1[] = " seeds in read no. ";
+    static const char h2[] = " (Read[begin, End] -> starting position(s) on the reference)"
+                             "===================================*/\n";
+    for (uint32_t r = 0; r < c->n_reads; r++) {
+        ob_put(&o, h0, sizeof(h0) - 1);
+        if (smem) ob_put(&o, "SMEM", 4);
+        else ob_put(&o, "MEM", 3);
+        ob_put(&o, h1, sizeof(h1) - 1);
+        ob_u32(&o, first_read_no + r);
+        ob_put(&o, h2, sizeof(h2) - 1);
+        const uint32_t *pos = c->h_pos + c->h_pos_off[r];
+        for (uint64_t s = c->h_seed_off[r]; s < c->h_seed_off[r + 1]; s++) {
+            const gs_seed_rec &S = c->h_seeds[s];
+            char sg = ((uint32_t)S.y >> 31) ? '-' : '+';
+            for (uint32_t q = 0; q < S.n_pos; q++, pos++) {
+                if (q == 0) {
+                    ob_put(&o, "\nRead[", 6);
+                    ob_u32(&o, (uint32_t)S.x & 0x7fffffffu);
+                    ob_put(&o, ", ", 2);
+                    ob_u32(&o, (uint32_t)S.y & 0x7fffffffu);
+                    ob_put(&o, "] -> ", 5);
+                } else {
+                    ob_put(&o, ", ", 2);
+                }
+                ob_put(&o, &sg, 1);
+                ob_u32(&o, *pos);
+            }
+        }
+        ob_put(&o, "\n", 1);
+    }
+    ob_flush(&o);
+    free(o.b);
+    if (o.err) {
+        gs_set_error("write failed");
+        return GS_EIO;
+    }
+    return GS_OK;
+}

@@ -1,0 +1,94 @@
+/*
+ * gs_internal.h -- device data layout and helpers shared by the kernels.
+ */
+#ifndef GS_INTERNAL_H
+#define GS_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/gpuseed.h"
+
+#define GS_OCC_INTERVAL 64u   /* rows per occurrence block (seed_gen.cu:29) */
+#define GS_BLOCK_WORDS 8u     /* 4 counts + 4 two-bit BWT words = 32 bytes */
+#define GS_K0 13              /* k-mer table length (seed_gen.cu:2822) */
+#define GS_HIST 8             /* containment history depth of the batched search */
+#define GS_CHUNK 31           /* candidates owned by one warp work item */
+
+/* Device view of the index, passed by value to every kernel.
+ * occ: one 32-byte block per 64 rows of the $-removed BWT string:
+ *      {count of A, C, G, T before the block, 4 words of 16 bases, MSB first}.
+ * sa:  sampled suffix array, sa[0] = 0xffffffff (the $ row).
+ * kmer: (l,u) of every 13-mer, base j at bits 2j, processed first. */
+struct GsDevIndex {
+    const uint32_t *occ;
+    const uint32_t *sa;
+    const uint2 *kmer;
+    uint32_t primary, seq_len, sa_intv, n_sa;
+    uint32_t L2[5];
+};
+
+/* Candidate slot written by the search kernels; y == 0 marks "no record". */
+struct GsRec {
+    int32_t x, y;
+    uint32_t l, u;
+};
+
+/* Per-batch device arguments shared by the pipeline kernels. */
+struct GsBatch {
+    const char *seqs;          /* ASCII bases */
+    const uint64_t *offsets;   /* per read */
+    const uint32_t *lengths;   /* per read */
+    uint32_t n_reads;
+    int32_t k, smem, n_mode, lf_mode;
+    uint64_t *slot_off;        /* per read (n+1): first candidate slot */
+    uint32_t *item_off;        /* per read (n+1): first work item */
+    GsRec *slots;              /* 2 * candidates */
+    uint32_t *hist;            /* plain kernel: one word per base */
+    uint32_t *rd_nf, *rd_nr;   /* per read: compacted record counts */
+    uint64_t *rd_nseeds, *rd_npos;   /* per read counts ... */
+    uint64_t *seed_off, *pos_off;    /* ... and their exclusive scans (n+1) */
+    gs_seed_rec *seeds;            /* output seeds */
+    uint64_t *seed_pos;        /* per output seed: index of its first position */
+    uint32_t *pos;             /* output positions */
+    uint32_t *pmap;            /* position -> seed */
+    uint64_t seed_cap, pos_cap;
+    uint32_t *queue;           /* [0]: work-queue head, [1]: status flags */
+};
+
+#define GS_FLAG_WALK 1u
+#define GS_FLAG_OVERFLOW 2u
+
+__host__ __device__ static inline uint32_t gs_fwd_code(unsigned char ch)
+{
+    /* pack_4bit_fow table (seed_gen.cu:2539): A0 C1 G2 T3 N4, others 0/5 */
+    return (0x24031005u >> ((ch & 7u) << 2)) & 15u;
+}
+
+__host__ __device__ static inline uint32_t gs_comp_code(unsigned char ch)
+{
+    /* pack_4bit_rev table (seed_gen.cu:2561): complement codes */
+    return (0x14002035u >> ((ch & 7u) << 2)) & 15u;
+}
+
+/* host helpers (gs_api.cu) */
+void gs_set_error(const char *fmt, ...);
+int gs_cuda_fail(cudaError_t e, const char *what);
+#define GS_CUDA(call)                                         \
+    do {                                                      \
+        cudaError_t _e = (call);                              \
+        if (_e != cudaSuccess) return gs_cuda_fail(_e, #call); \
+    } while (0)
+
+/* kernel launchers (defined next to their kernels) */
+int gs_build_kmer_table(const GsDevIndex &idx, uint2 *table, cudaStream_t st);
+int gs_launch_search(const GsDevIndex &idx, GsBatch &b, int kernel, int queue_chunk,
+                     int ctas_per_sm, uint32_t n_items, cudaStream_t st);
+int gs_launch_prepare(GsBatch &b, cudaStream_t st);
+int gs_launch_finalize_count(const GsDevIndex &idx, GsBatch &b, cudaStream_t st);
+int gs_launch_finalize_emit(const GsDevIndex &idx, GsBatch &b, cudaStream_t st);
+int gs_launch_locate(const GsDevIndex &idx, GsBatch &b, uint64_t n_seeds, uint64_t n_pos,
+                     cudaStream_t st);
+
+#endif

@@ -1,0 +1,250 @@
+/*
+ * gs_post.cu -- per-read filtering, ordering and the sampled-SA locate.
+ *
+ * Replaces, for one batch, the reference's compaction (DeviceSelect::Flagged,
+ * seed_gen.cu:3400-3401), the SMEM/MEM filters and counts (:865-1251), the
+ * segmented sorts by begin (:1233, :3570) and the expansion + locate kernels
+ * (:555-724):
+ *
+ *   gs_finalize_count  warp per read: compacts the read's candidate slots in
+ *                      place (ballot prefix) and counts the seeds/positions
+ *                      the filters keep;
+ *   (scan)             exclusive sums of those counts over reads;
+ *   gs_finalize_emit   thread per read: merges the forward (ascending end)
+ *                      and reverse (ascending start) records by begin --
+ *                      equal begins keep forward first, as the reference's
+ *                      stable sort does -- and writes the output seeds;
+ *   gs_expand          position -> seed map;
+ *   gs_locate          thread per position: LF walk to a sampled row.
+ *
+ * Filter rules on the per-strand record lists (ascending end / start):
+ *   SMEM forward: keep a record unless the next one has the same begin
+ *        (:1000-1006); reverse: keep unless the previous has the same end
+ *        (:1013-1019).
+ *   MEM  forward: drop a record whose next record has the same begin and the
+ *        same interval size (:1114-1120); its positions are its rows minus the
+ *        rows of that next same-begin record's interval (:933-953, :624-667);
+ *        reverse: the same toward the previous record with the same end.
+ */
+#include "gs_fm.cuh"
+
+
+
+__device__ __forceinline__ uint32_t gs_size(const GsRec &r) { return r.u - r.l + 1u; }
+
+/* decision for forward record o of list F[0..nf) */
+__device__ __forceinline__ void gs_fwd_rule(const GsRec *F, uint32_t nf, uint32_t o, int smem,
+                                            bool &keep, uint32_t &cnt, uint32_t &xl, uint32_t &xu)
+{
+    GsRec R = F[o];
+    bool same = false;
+    GsRec N;
+    N.l = 1; N.u = 0; N.x = 0; N.y = 0;
+    if (o + 1 < nf) {
+        N = F[o + 1];
+        same = N.x == R.x;
+    }
+    uint32_t sz = gs_size(R);
+    xl = 1; xu = 0;
+    if (smem) {
+        keep = !same;
+        cnt = sz;
+    } else {
+        uint32_t nsz = same ? gs_size(N) : 0u;
+        keep = !(same && nsz == sz);
+        cnt = sz - nsz;
+        if (same) { xl = N.l; xu = N.u; }
+    }
+}
+
+__device__ __forceinline__ void gs_rev_rule(const GsRec *Rv, uint32_t nr, uint32_t o, int smem,
+                                            bool &keep, uint32_t &cnt, uint32_t &xl, uint32_t &xu)
+{
+    (void)nr;
+    GsRec R = Rv[o];
+    bool same = false;
+    GsRec P;
+    P.l = 1; P.u = 0; P.x = 0; P.y = 0;
+    if (o > 0) {
+        P = Rv[o - 1];
+        same = P.y == R.y;
+    }
+    uint32_t sz = gs_size(R);
+    xl = 1; xu = 0;
+    if (smem) {
+        keep = !same;
+        cnt = sz;
+    } else {
+        uint32_t psz = same ? gs_size(P) : 0u;
+        keep = !(same && psz == sz);
+        cnt = sz - psz;
+        if (same) { xl = P.l; xu = P.u; }
+    }
+}
+
+/* compacts slots[0..n) (y != 0) to the front, in order; returns the count */
+__device__ __forceinline__ uint32_t gs_warp_compact(GsRec *s, uint32_t n, int lane)
+{
+    uint32_t cnt = 0;
+    for (uint32_t c0 = 0; c0 < n; c0 += 32) {
+        uint32_t i = c0 + (uint32_t)lane;
+        GsRec r;
+        bool v = false;
+        if (i < n) {
+            r = s[i];
+            v = r.y != 0;
+        }
+        uint32_t m = __ballot_sync(0xffffffffu, v);
+        __syncwarp();
+        if (v) s[cnt + __popc(m & ((1u << lane) - 1u))] = r;
+        __syncwarp();
+        cnt += __popc(m);
+    }
+    return cnt;
+}
+
+__global__ void __launch_bounds__(256) gs_finalize_count(GsBatch B)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t r = warp; r < B.n_reads; r += nwarps) {
+        uint64_t base = B.slot_off[r];
+        uint32_t n = (uint32_t)((B.slot_off[r + 1] - base) >> 1);
+        GsRec *F = B.slots + base;
+        GsRec *Rv = F + n;
+        uint32_t nf = gs_warp_compact(F, n, lane);
+        uint32_t nr = gs_warp_compact(Rv, n, lane);
+        uint64_t seeds = 0, npos = 0;
+        for (uint32_t o = lane; o < nf; o += 32) {
+            bool keep; uint32_t cnt, xl, xu;
+            gs_fwd_rule(F, nf, o, B.smem, keep, cnt, xl, xu);
+            if (keep && cnt) { seeds++; npos += cnt; }
+        }
+        for (uint32_t o = lane; o < nr; o += 32) {
+            bool keep; uint32_t cnt, xl, xu;
+            gs_rev_rule(Rv, nr, o, B.smem, keep, cnt, xl, xu);
+            if (keep && cnt) { seeds++; npos += cnt; }
+        }
+        for (int off = 16; off; off >>= 1) {
+            seeds += __shfl_xor_sync(0xffffffffu, seeds, off);
+            npos += __shfl_xor_sync(0xffffffffu, npos, off);
+        }
+        if (lane == 0) {
+            B.rd_nf[r] = nf;
+            B.rd_nr[r] = nr;
+            B.rd_nseeds[r] = seeds;
+            B.rd_npos[r] = npos;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) gs_finalize_emit(GsBatch B, uint64_t *seed_pos)
+{
+    uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= B.n_reads) return;
+    uint64_t base = B.slot_off[r];
+    uint32_t n = (uint32_t)((B.slot_off[r + 1] - base) >> 1);
+    const GsRec *F = B.slots + base;
+    const GsRec *Rv = F + n;
+    uint32_t nf = B.rd_nf[r], nr = B.rd_nr[r];
+    uint64_t s = B.seed_off[r];
+    uint64_t p = B.pos_off[r];
+    uint32_t a = 0, b = 0;
+    while (a < nf || b < nr) {
+        bool take_f;
+        if (a >= nf) take_f = false;
+        else if (b >= nr) take_f = true;
+        else take_f = ((uint32_t)F[a].x & 0x7fffffffu) <= ((uint32_t)Rv[b].x & 0x7fffffffu);
+        bool keep; uint32_t cnt, xl, xu;
+        GsRec R;
+        if (take_f) {
+            gs_fwd_rule(F, nf, a, B.smem, keep, cnt, xl, xu);
+            R = F[a++];
+        } else {
+            gs_rev_rule(Rv, nr, b, B.smem, keep, cnt, xl, xu);
+            R = Rv[b++];
+        }
+        if (keep && cnt) {
+            if (s < B.seed_cap) {
+                gs_seed_rec o;
+                o.x = R.x; o.y = R.y; o.l = R.l; o.u = R.u;
+                o.xl = xl; o.xu = xu; o.n_pos = cnt; o.pad = 0;
+                B.seeds[s] = o;
+                seed_pos[s] = p;
+            }
+            s++;
+            p += cnt;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) gs_expand(const uint64_t *seed_pos, const gs_seed_rec *seeds,
+                                                 uint64_t n_seeds, uint32_t *pmap)
+{
+    uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_seeds) return;
+    uint64_t p = seed_pos[s];
+    uint32_t n = seeds[s].n_pos;
+    for (uint32_t i = 0; i < n; i++) pmap[p + i] = (uint32_t)s;
+}
+
+__global__ void __launch_bounds__(256) gs_locate(GsDevIndex I, const gs_seed_rec *seeds,
+                                                 const uint64_t *seed_pos, const uint32_t *pmap,
+                                                 uint64_t n_pos, uint32_t *out, int lf_mode,
+                                                 uint32_t *flags)
+{
+    uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_pos) return;
+    uint32_t s = pmap[j];
+    gs_seed_rec S = seeds[s];
+    uint32_t row = S.l + (uint32_t)(j - seed_pos[s]);
+    if (S.xl <= S.xu && row >= S.xl) row += S.xu - S.xl + 1u;
+    /* locate_seeds_gpu (:668-684): LF until a sampled row; a consistent
+     * index reaches one within seq_len+1 steps */
+    uint32_t steps = 0;
+    const uint32_t cap = I.seq_len + 2u;
+    while (row % I.sa_intv) {
+        row = gs_lf(I, row, lf_mode);
+        if (++steps > cap) {
+            atomicOr(flags, GS_FLAG_WALK);
+            out[j] = 0xffffffffu;
+            return;
+        }
+    }
+    out[j] = __ldg(&I.sa[row / I.sa_intv]) + steps;
+}
+
+int gs_launch_finalize_count(const GsDevIndex &I, GsBatch &B, cudaStream_t st)
+{
+    (void)I;
+    if (B.n_reads == 0) return GS_OK;
+    uint32_t grid = (B.n_reads + 7) / 8;
+    if (grid > 152u * 16u) grid = 152u * 16u;
+    gs_finalize_count<<<grid, 256, 0, st>>>(B);
+    GS_CUDA(cudaGetLastError());
+    return GS_OK;
+}
+
+int gs_launch_finalize_emit(const GsDevIndex &I, GsBatch &B, cudaStream_t st)
+{
+    (void)I;
+    if (B.n_reads == 0) return GS_OK;
+    gs_finalize_emit<<<(B.n_reads + 127) / 128, 128, 0, st>>>(B, B.seed_pos);
+    GS_CUDA(cudaGetLastError());
+    return GS_OK;
+}
+
+int gs_launch_locate(const GsDevIndex &I, GsBatch &B, uint64_t n_seeds, uint64_t n_pos,
+                     cudaStream_t st)
+{
+    if (n_seeds == 0 || n_pos == 0) return GS_OK;
+    gs_expand<<<(unsigned)((n_seeds + 255) / 256), 256, 0, st>>>(B.seed_pos, B.seeds, n_seeds,
+                                                                  B.pmap);
+    GS_CUDA(cudaGetLastError());
+    gs_locate<<<(unsigned)((n_pos + 255) / 256), 256, 0, st>>>(I, B.seeds, B.seed_pos, B.pmap,
+                                                                n_pos, B.pos, B.lf_mode,
+                                                                B.queue + 1);
+    GS_CUDA(cudaGetLastError());
+    return GS_OK;
+}

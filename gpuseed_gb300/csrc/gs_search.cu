@@ -1,0 +1,337 @@
+/*
+ * gs_search.cu -- seed-interval search (the hot path).
+ *
+ * Semantics (restated from find_seed_intervals_gpu, seed_gen.cu:2087-2413):
+ *   forward candidate e (end):   13-mer R[e-12..e] from the k-mer table, then
+ *                                extend left while the interval stays valid;
+ *                                record ([b, e+1), I) if e+1-b >= k;
+ *   reverse candidate s (start): complement codes, 13-mer at s, extend right;
+ *                                record ([s, x+1) | bit 31, I) if x+1-s >= k.
+ * A candidate may stop early once its interval has the same size as that of
+ * its neighbour toward the longer match (e+1 forward, s-1 reverse) at the
+ * same far end: both filters drop such a record, so it need not be produced.
+ * The reference prunes with 30 warp shuffles per step over uninitialised
+ * flags (:2100-2204); this file uses a defined rule: compare with the nearest
+ * still-extending lane to the right, from a GS_HIST-deep own history.
+ *
+ * Two launch forms:
+ *   gs_search_batched: persistent CTAs; each warp takes work items
+ *     (read, strand, 31 candidates + 1 helper lane) from a global queue and
+ *     steps its 32 candidates in lockstep, one occ lookup per lane per step.
+ *   gs_search_plain:   one thread per read, candidates one after another,
+ *     containment history in a per-read global array.
+ */
+#include "gs_fm.cuh"
+
+
+
+/* ------------------------------------------------------------------ */
+/* 13-mer interval table (pre_calc_seed_intervals_gpu, seed_gen.cu:2648) */
+
+__global__ void gs_kmer_kernel(GsDevIndex I, uint2 *table, uint32_t n)
+{
+    uint32_t patt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (patt >= n) return;
+    uint32_t l = 0, u = I.seq_len;
+    for (int i = 0; i < GS_K0; i++) {
+        gs_step(I, l, u, (patt >> (i << 1)) & 3u);
+        if (l > u) break;
+    }
+    table[patt] = make_uint2(l, u);
+}
+
+int gs_build_kmer_table(const GsDevIndex &I, uint2 *table, cudaStream_t st)
+{
+    uint32_t n = 1u << (2 * GS_K0);
+    gs_kmer_kernel<<<(n + 255) / 256, 256, 0, st>>>(I, table, n);
+    GS_CUDA(cudaGetLastError());
+    return GS_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* per-batch preparation: candidate slots and work items per read */
+
+__global__ void gs_prepare_kernel(const uint32_t *lengths, uint32_t n_reads, int k,
+                                  uint64_t *slot_n, uint32_t *item_n)
+{
+    uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > n_reads) return;
+    uint32_t n = 0;
+    if (r < n_reads && lengths[r] >= (uint32_t)k) n = lengths[r] - (uint32_t)k + 1u;
+    slot_n[r] = 2ull * n;
+    item_n[r] = 2u * ((n + GS_CHUNK - 1) / GS_CHUNK);
+}
+
+int gs_launch_prepare(GsBatch &b, cudaStream_t st)
+{
+    uint32_t n = b.n_reads + 1;
+    /* counts are written in place and scanned into offsets */
+    gs_prepare_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.lengths, b.n_reads, b.k, b.slot_off,
+                                                        b.item_off);
+    GS_CUDA(cudaGetLastError());
+    return GS_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* batched search */
+
+template <int NSTOP>
+__device__ __forceinline__ void gs_warp_item(const GsDevIndex &I, const GsBatch &B, uint32_t r,
+                                             uint32_t local, int lane)
+{
+    const uint32_t L = B.lengths[r];
+    const int k = B.k;
+    const uint32_t n = L - (uint32_t)k + 1u;
+    const uint32_t nch = (n + GS_CHUNK - 1) / GS_CHUNK;
+    const bool fwd = local < nch;
+    const uint32_t chunk = fwd ? local : local - nch;
+    const uint32_t ci = chunk * GS_CHUNK + (uint32_t)lane;
+    const bool in_range = ci < n;
+    const bool owned = in_range && (lane < GS_CHUNK || ci == n - 1u);
+    const unsigned char *seq = (const unsigned char *)B.seqs + B.offsets[r];
+    const int iL = (int)L;
+
+    /* anchor: e = k-1+ci (fwd), s = n-1-ci (rev); the containing neighbour
+     * of every lane is lane+1 */
+    int anchor = fwd ? (k - 1 + (int)ci) : ((int)n - 1 - (int)ci);
+    uint32_t l = 1, u = 0;
+    bool ok = in_range;
+    uint32_t pat = 0;
+    if (in_range) {
+#pragma unroll
+        for (int j = 0; j < GS_K0; j++) {
+            uint32_t c = fwd ? gs_fwd_code(seq[anchor - j]) : gs_comp_code(seq[anchor + j]);
+            ok = ok && c <= 3u;
+            pat |= (c & 3u) << (j << 1);
+        }
+    }
+    if (ok) {
+        uint2 iv = __ldg(&I.kmer[pat]);
+        l = iv.x;
+        u = iv.y;
+    }
+    bool alive = ok && l <= u;
+    int pos = fwd ? anchor - (GS_K0 - 1) : anchor + (GS_K0 - 1);
+    const int dir = fwd ? -1 : 1;
+
+    uint32_t hist[GS_HIST];
+#pragma unroll
+    for (int m = 0; m < GS_HIST; m++) hist[m] = 0;
+    uint32_t cur = alive ? u - l + 1u : 0u;
+    bool killed = false;
+    int t = 0;
+    const uint32_t owned_mask = __ballot_sync(0xffffffffu, owned);
+
+    while (__ballot_sync(0xffffffffu, alive) & owned_mask) {
+        if (alive) {
+            int np = pos + dir;
+            if (np < 0 || np >= iL) {
+                alive = false;
+            } else {
+                uint32_t c = fwd ? gs_fwd_code(seq[np]) : gs_comp_code(seq[np]);
+                if (c > 3u) {
+                    if (NSTOP) alive = false;
+                    else pos = np;               /* wildcard: interval unchanged */
+                } else {
+                    uint32_t nl = l, nu = u;
+                    gs_step(I, nl, nu, c);
+                    if (nl > nu) {
+                        alive = false;
+                    } else {
+                        l = nl;
+                        u = nu;
+                        pos = np;
+                    }
+                }
+            }
+        }
+        t++;
+        uint32_t pub = alive ? u - l + 1u : 0u;
+        /* containment: own size d steps ago vs the nearest extending lane
+         * d to the right, which now stands at the same far end */
+        uint32_t right = __ballot_sync(0xffffffffu, pub != 0u) & ~((2u << lane) - 1u);
+        int j = right ? __ffs(right) - 1 : lane;
+        uint32_t v = __shfl_sync(0xffffffffu, pub, j);
+        int d = j - lane;
+        if (alive && right && d <= GS_HIST && d <= t) {
+            /* cur = own size one step ago, hist[m] = m+2 steps ago */
+            uint32_t h = cur;
+#pragma unroll
+            for (int m = 0; m < GS_HIST - 1; m++) h = (d == m + 2) ? hist[m] : h;
+            if (h == v) {
+                alive = false;
+                killed = true;
+            }
+        }
+#pragma unroll
+        for (int m = GS_HIST - 1; m > 0; m--) hist[m] = hist[m - 1];
+        hist[0] = cur;
+        cur = pub;
+    }
+
+    if (owned) {
+        GsRec rec;
+        rec.x = 0; rec.y = 0; rec.l = l; rec.u = u;
+        if (!killed) {
+            if (fwd) {
+                /* length e - beg with beg = pos-1; a 13-mer that is absent
+                 * still counts 13 (the k == 13 case of :2259) */
+                int len = anchor - pos + 1;
+                if (ok && len >= k) {
+                    rec.x = pos;
+                    rec.y = anchor + 1;
+                }
+            } else if (ok && l <= u) {
+                int len = pos + 1 - anchor;
+                if (len >= k) {
+                    rec.x = (int32_t)((uint32_t)anchor | 0x80000000u);
+                    rec.y = (int32_t)((uint32_t)(pos + 1) | 0x80000000u);
+                }
+            }
+        }
+        uint64_t slot = B.slot_off[r] + (fwd ? (uint64_t)(anchor - (k - 1)) : (uint64_t)n + (uint64_t)anchor);
+        B.slots[slot] = rec;
+    }
+}
+
+template <int NSTOP>
+__global__ void __launch_bounds__(256) gs_search_batched(GsDevIndex I, GsBatch B, uint32_t n_items,
+                                                         int queue_chunk)
+{
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t first = 0;
+        if (lane == 0) first = atomicAdd(B.queue, (uint32_t)queue_chunk);
+        first = __shfl_sync(0xffffffffu, first, 0);
+        if (first >= n_items) break;
+        uint32_t last = min(first + (uint32_t)queue_chunk, n_items);
+        /* read of the first item: largest r with item_off[r] <= first */
+        uint32_t lo = 0, hi = B.n_reads;
+        while (lo + 1 < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (B.item_off[mid] <= first) lo = mid; else hi = mid;
+        }
+        uint32_t r = lo;
+        for (uint32_t it = first; it < last; it++) {
+            while (B.item_off[r + 1] <= it) r++;
+            gs_warp_item<NSTOP>(I, B, r, it - B.item_off[r], lane);
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* plain search: one read per thread */
+
+template <int NSTOP>
+__global__ void __launch_bounds__(128) gs_search_plain(GsDevIndex I, GsBatch B)
+{
+    uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= B.n_reads) return;
+    const uint32_t L = B.lengths[r];
+    const int k = B.k;
+    if (L < (uint32_t)k) return;
+    const uint32_t n = L - (uint32_t)k + 1u;
+    const unsigned char *seq = (const unsigned char *)B.seqs + B.offsets[r];
+    uint32_t *H = B.hist + B.offsets[r];
+    GsRec *slots = B.slots + B.slot_off[r];
+    const int iL = (int)L;
+
+    for (int strand = 0; strand < 2; strand++) {
+        const bool fwd = strand == 0;
+        for (uint32_t q = 0; q < L; q++) H[q] = 0;
+        for (uint32_t ci = 0; ci < n; ci++) {
+            /* forward: e from L-1 down; reverse: s from 0 up */
+            int anchor = fwd ? iL - 1 - (int)ci : (int)ci;
+            uint32_t pat = 0;
+            bool ok = true;
+            for (int j = 0; j < GS_K0; j++) {
+                uint32_t c = fwd ? gs_fwd_code(seq[anchor - j]) : gs_comp_code(seq[anchor + j]);
+                if (c > 3u) { ok = false; break; }
+                pat |= c << (j << 1);
+            }
+            uint32_t l = 1, u = 0;
+            if (ok) {
+                uint2 iv = __ldg(&I.kmer[pat]);
+                l = iv.x;
+                u = iv.y;
+            }
+            int pos = fwd ? anchor - (GS_K0 - 1) : anchor + (GS_K0 - 1);
+            bool killed = false;
+            if (ok && l <= u) {
+                uint32_t sz = u - l + 1u;
+                uint32_t h = H[pos];
+                H[pos] = sz;
+                killed = (h == sz);
+                const int dir = fwd ? -1 : 1;
+                while (!killed) {
+                    int np = pos + dir;
+                    if (np < 0 || np >= iL) break;
+                    uint32_t c = fwd ? gs_fwd_code(seq[np]) : gs_comp_code(seq[np]);
+                    uint32_t nl = l, nu = u;
+                    if (c > 3u) {
+                        if (NSTOP) break;
+                    } else {
+                        gs_step(I, nl, nu, c);
+                        if (nl > nu) break;
+                    }
+                    l = nl;
+                    u = nu;
+                    pos = np;
+                    sz = u - l + 1u;
+                    h = H[pos];
+                    H[pos] = sz;
+                    killed = (h == sz);
+                }
+            }
+            GsRec rec;
+            rec.x = 0; rec.y = 0; rec.l = l; rec.u = u;
+            if (!killed && ok) {
+                if (fwd) {
+                    if (anchor - pos + 1 >= k) { rec.x = pos; rec.y = anchor + 1; }
+                } else if (l <= u && pos + 1 - anchor >= k) {
+                    rec.x = (int32_t)((uint32_t)anchor | 0x80000000u);
+                    rec.y = (int32_t)((uint32_t)(pos + 1) | 0x80000000u);
+                }
+            }
+            uint64_t slot = fwd ? (uint64_t)(anchor - (k - 1)) : (uint64_t)n + (uint64_t)anchor;
+            slots[slot] = rec;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+
+int gs_launch_search(const GsDevIndex &I, GsBatch &B, int kernel, int queue_chunk, int ctas_per_sm,
+                     uint32_t n_items, cudaStream_t st)
+{
+    if (B.n_reads == 0) return GS_OK;
+    if (kernel == GS_KERNEL_PLAIN) {
+        uint32_t nb = (B.n_reads + 127) / 128;
+        if (B.n_mode == GS_N_STOP) gs_search_plain<1><<<nb, 128, 0, st>>>(I, B);
+        else gs_search_plain<0><<<nb, 128, 0, st>>>(I, B);
+        GS_CUDA(cudaGetLastError());
+        return GS_OK;
+    }
+    int dev = 0, sms = 0;
+    GS_CUDA(cudaGetDevice(&dev));
+    GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (queue_chunk <= 0) queue_chunk = 2;
+    if (ctas_per_sm <= 0) {
+        int occ = 0;
+        if (B.n_mode == GS_N_STOP)
+            GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gs_search_batched<1>, 256, 0));
+        else
+            GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gs_search_batched<0>, 256, 0));
+        ctas_per_sm = occ > 0 ? occ : 1;
+    }
+    uint32_t grid = (uint32_t)sms * (uint32_t)ctas_per_sm;
+    uint32_t need = (n_items + (uint32_t)queue_chunk - 1) / (uint32_t)queue_chunk;
+    uint32_t warps = grid * 8;
+    if (need < warps) grid = (need + 7) / 8;
+    if (grid == 0) grid = 1;
+    GS_CUDA(cudaMemsetAsync(B.queue, 0, sizeof(uint32_t), st));
+    if (B.n_mode == GS_N_STOP) gs_search_batched<1><<<grid, 256, 0, st>>>(I, B, n_items, queue_chunk);
+    else gs_search_batched<0><<<grid, 256, 0, st>>>(I, B, n_items, queue_chunk);
+    GS_CUDA(cudaGetLastError());
+    return GS_OK;
+}

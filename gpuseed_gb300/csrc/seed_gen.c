@@ -1,0 +1,153 @@
+/*
+ * seed_gen.c -- drop-in for the reference's seed_gen executable.
+ *
+ *   seed_gen [-k INT] [-s] [-o] <index prefix> <reads.fa>
+ *
+ * Same options (getopt "k:so", seed_gen.cu:2826-2839), same index files and
+ * the same stdout records (seed_gen.cu:3625-3647).  FASTA handling follows
+ * the reference's getline loop (seed_gen.cu:2955-2990): lines starting with
+ * '>' are skipped, every other line is one read whose last character (the
+ * newline) is dropped.  Reads are processed in batches of at least
+ * BATCH_BASES bases, numbered from 1 across batches.
+ *
+ * Extra options, off by default: -n (a non-ACGT base stops the extension),
+ * -b (bwa's LF at row primary+1), -P (one-read-per-thread search kernel),
+ * -B INT (bases per batch).  Errors print a message and exit with status 1,
+ * as the reference does for unreadable index files.
+ */
+#define _GNU_SOURCE
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/time.h>
+#include <unistd.h>
+
+#include "../../include/gpuseed.h"
+
+static double now_s(void)
+{
+    struct timeval tv;
+    gettimeofday(&tv, NULL);
+    return tv.tv_sec + tv.tv_usec * 1e-6;
+}
+
+static void die(const char *what, int rc)
+{
+    fprintf(stderr, "seed_gen: %s: %s (%s)\n", what, gs_strerror(rc), gs_last_error());
+    exit(1);
+}
+
+int main(int argc, char *argv[])
+{
+    double t_start = now_s();
+    gs_params p;
+    memset(&p, 0, sizeof(p));
+    p.k = 20;
+    uint64_t batch_bases = 64u << 20;
+    int print_out = 0, c;
+    while ((c = getopt(argc, argv, "k:sonbPB:")) >= 0) {
+        switch (c) {
+        case 'k': p.k = atoi(optarg); break;
+        case 's': p.smem = 1; break;
+        case 'o': print_out = 1; break;
+        case 'n': p.n_mode = GS_N_STOP; break;
+        case 'b': p.lf_mode = GS_LF_BWA; break;
+        case 'P': p.kernel = GS_KERNEL_PLAIN; break;
+        case 'B': batch_bases = strtoull(optarg, NULL, 10); break;
+        default: break;
+        }
+    }
+    if (optind + 2 > argc) {
+        fprintf(stderr, "Usage: seed_gen [-k <minimum seed length>] [-s] [-o] <index prefix> "
+                        "<reads fasta file>\n");
+        return 1;
+    }
+    fprintf(stderr, "Loading index from file and copying it to GPU...\n");
+    double t0 = now_s();
+    gs_index *idx = NULL;
+    int rc = gs_index_load(argv[optind], 0, &idx);
+    if (rc) die("loading index", rc);
+    gs_index_info info;
+    gs_index_get_info(idx, &info);
+    fprintf(stderr, "seq_len=%u primary=%u sa_intv=%u; index and 13-mer table on GPU in %.3f s\n",
+            info.seq_len, info.primary, info.sa_intv, now_s() - t0);
+    gs_ctx *ctx = NULL;
+    rc = gs_ctx_create(idx, NULL, &ctx);
+    if (rc) die("creating context", rc);
+
+    FILE *fp = fopen(argv[optind + 1], "r");
+    if (!fp) {
+        fprintf(stderr, "seed_gen: cannot open %s\n", argv[optind + 1]);
+        return 1;
+    }
+    size_t cap_b = 1 << 20, cap_r = 1 << 16;
+    char *bases = (char *)malloc(cap_b);
+    uint64_t *offs = (uint64_t *)malloc(cap_r * 8);
+    uint32_t *lens = (uint32_t *)malloc(cap_r * 4);
+    char *line = NULL;
+    size_t line_cap = 0;
+    uint32_t reads_done = 0;
+    double t_gpu = 0, t_load = 0, t_print = 0;
+    int all_done = 0;
+    while (!all_done) {
+        double tl = now_s();
+        uint64_t nb = 0;
+        uint32_t nr = 0;
+        while (nb < batch_bases) {
+            ssize_t n = getline(&line, &line_cap, fp);
+            if (n < 0) {
+                all_done = 1;
+                break;
+            }
+            if (line[0] == '>') continue;
+            size_t L = n > 0 ? (size_t)n - 1 : 0;
+            if (nb + L + 1 > cap_b) {
+                while (nb + L + 1 > cap_b) cap_b *= 2;
+                bases = (char *)realloc(bases, cap_b);
+            }
+            if (nr + 1 > cap_r) {
+                cap_r *= 2;
+                offs = (uint64_t *)realloc(offs, cap_r * 8);
+                lens = (uint32_t *)realloc(lens, cap_r * 4);
+            }
+            if (!bases || !offs || !lens) {
+                fprintf(stderr, "seed_gen: out of host memory\n");
+                return 1;
+            }
+            memcpy(bases + nb, line, L);
+            offs[nr] = nb;
+            lens[nr] = (uint32_t)L;
+            nb += L;
+            nr++;
+        }
+        t_load += now_s() - tl;
+        if (nr == 0) break;
+        double tg = now_s();
+        rc = gs_seed(ctx, bases, offs, lens, nr, &p);
+        if (rc) die("seeding batch", rc);
+        t_gpu += now_s() - tg;
+        gs_result_view v;
+        gs_result_host(ctx, &v);
+        fprintf(stderr, "batch of %u reads: %llu seeds, %llu positions, %.3f s on GPU\n", nr,
+                (unsigned long long)v.n_seeds, (unsigned long long)v.n_pos, now_s() - tg);
+        if (print_out) {
+            double tp = now_s();
+            fflush(stdout);
+            rc = gs_result_write_text(ctx, 1, reads_done + 1, p.smem);
+            if (rc) die("writing records", rc);
+            t_print += now_s() - tp;
+        }
+        reads_done += nr;
+    }
+    fclose(fp);
+    free(line);
+    free(bases);
+    free(offs);
+    free(lens);
+    gs_ctx_free(ctx);
+    gs_index_free(idx);
+    fprintf(stderr, "%s seeds: %u reads, GPU time %.3f s, load %.3f s, print %.3f s, total %.3f s\n",
+            p.smem ? "SMEM" : "MEM", reads_done, t_gpu, t_load, t_print, now_s() - t_start);
+    return 0;
+}

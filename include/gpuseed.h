@@ -1,0 +1,143 @@
+/*
+ * gpuseed.h -- C-ABI of the GB300 seeding library (libgpuseed.so).
+ *
+ * The reference (nahmedraja/GPUseed) has no library interface: its boundary is
+ * the seed_gen process, the .bwt/.sa index files and the text records on
+ * stdout (seed_gen.cu:2817-3815).  These entry points are what a caller of
+ * that path binds instead; each comment names the reference code it replaces.
+ * Plain pointers and sizes only.  Every call returns 0 or a negative GS_E*
+ * code and never exits; gs_last_error() describes the last failure of the
+ * calling thread.
+ *
+ * Threading: a gs_index is immutable after loading and may be shared by
+ * threads; a gs_ctx (stream + workspace + last result) belongs to one host
+ * thread at a time.
+ */
+#ifndef GPUSEED_H
+#define GPUSEED_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GS_OK 0
+#define GS_EINVAL -1     /* bad argument */
+#define GS_EIO -2        /* file cannot be opened or read */
+#define GS_EFORMAT -3    /* index file truncated or inconsistent */
+#define GS_ENOMEM -4     /* device or host allocation failed / admission refused */
+#define GS_ECUDA -5      /* CUDA runtime error */
+#define GS_EWALK -6      /* sampled-SA walk exceeded its step limit (corrupt index) */
+#define GS_EOVERFLOW -7  /* output larger than the capacity given */
+#define GS_ETIMEOUT -8   /* a bounded wait ran out */
+#define GS_ESTATE -9     /* call not valid in the object's current state */
+
+/* Semantics switches (defaults first).  See the design doc for the reference
+ * behaviour each one reproduces. */
+#define GS_N_WILDCARD 0  /* non-ACGT base after the 13-mer: interval unchanged */
+#define GS_N_STOP 1      /* non-ACGT base stops the extension (bwa) */
+#define GS_LF_GPUSEED 0  /* LF(primary+1) = 0 as seed_gen.cu:455-458 */
+#define GS_LF_BWA 1      /* LF as bwa */
+
+#define GS_KERNEL_BATCHED 0 /* warp-cooperative persistent work-queue search */
+#define GS_KERNEL_PLAIN 1   /* one read per thread */
+
+typedef struct gs_index gs_index;
+typedef struct gs_ctx gs_ctx;
+
+/* seed_gen's -k / -s switches (seed_gen.cu:2820-2839) plus the quirk modes. */
+typedef struct {
+    int32_t k;          /* minimum seed length, >= 13 (default 20) */
+    int32_t smem;       /* 1: SMEM mode (-s); 0: MEM mode */
+    int32_t n_mode;     /* GS_N_WILDCARD | GS_N_STOP */
+    int32_t lf_mode;    /* GS_LF_GPUSEED | GS_LF_BWA */
+    int32_t kernel;     /* GS_KERNEL_BATCHED | GS_KERNEL_PLAIN */
+    int32_t queue_chunk;    /* work items a warp takes per queue grab (0 = auto) */
+    int32_t ctas_per_sm;    /* persistent CTAs per SM (0 = auto) */
+    int32_t reserved;
+} gs_params;
+
+/* One output seed, in output order.  x/y are the reference's int2 read
+ * position (begin, exclusive end; bit 31 of both set on the '-' strand,
+ * seed_gen.cu:2262, :2402).  Its positions are rows [l,u] minus the nested
+ * interval [xl,xu] (empty when xl > xu; MEM mode), n_pos of them. */
+typedef struct {
+    int32_t x, y;
+    uint32_t l, u;
+    uint32_t xl, xu;
+    uint32_t n_pos;
+    uint32_t pad;
+} gs_seed_rec;
+
+typedef struct {
+    uint32_t n_reads;
+    uint64_t n_seeds;
+    uint64_t n_pos;
+    const uint64_t *read_seed_off;  /* n_reads + 1 */
+    const uint64_t *read_pos_off;   /* n_reads + 1 */
+    const gs_seed_rec *seeds;           /* n_seeds */
+    const uint32_t *pos;            /* n_pos reference positions, output order */
+} gs_result_view;
+
+typedef struct {
+    uint32_t seq_len, primary, sa_intv, n_sa;
+    uint32_t L2[5];
+    int32_t device;
+    uint64_t device_bytes;          /* HBM held by the index */
+} gs_index_info;
+
+/* ---- index -------------------------------------------------------------
+ * Replaces bwt_restore_bwt / bwt_restore_sa + the H2D copies and the 13-mer
+ * table precalculation of seed_gen.cu:2685-2736, :2841-2895. */
+int gs_index_load(const char *prefix, int device, gs_index **out);
+/* Same from memory: .bwt words after the 5-word header and the .sa samples
+ * after its 7-word header. */
+int gs_index_from_host(uint32_t primary, const uint32_t L2_1to4[4], const uint32_t *bwt,
+                       uint64_t bwt_words, uint32_t sa_intv, const uint32_t *sa_samples,
+                       uint64_t n_samples, int device, gs_index **out);
+void gs_index_free(gs_index *idx);
+int gs_index_get_info(const gs_index *idx, gs_index_info *out);
+/* Copies the device 13-mer table (2*4^13 uint32: l,u per pattern) or a
+ * range of it to host memory (pre_calc_seed_intervals_gpu, seed_gen.cu:2648). */
+int gs_index_kmer_table(const gs_index *idx, uint64_t first, uint64_t count, uint32_t *out);
+/* Keeps the occurrence table in L2 under an access-policy window on every
+ * context stream (fraction of the set-aside, 0 disables). */
+int gs_index_set_l2_window(gs_index *idx, float hit_ratio);
+
+/* ---- seeding context ---------------------------------------------------
+ * One pass over a batch of reads replaces seed_gen's per-batch loop body
+ * (seed_gen.cu:3029-3620): pack, search, compaction, filters, sort, locate. */
+int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out);
+void gs_ctx_free(gs_ctx *ctx);
+/* Reads in host memory (ASCII, one record per read, offsets in bytes):
+ * copies them in, seeds, and copies the result back to host memory owned by
+ * the context (valid until the next call on it). */
+int gs_seed(gs_ctx *ctx, const char *seqs, const uint64_t *offsets, const uint32_t *lengths,
+            uint32_t n_reads, const gs_params *p);
+/* Reads already in device memory; fetch_to_host = 0 leaves the result on the
+ * device (gs_result_device). */
+int gs_seed_device(gs_ctx *ctx, const char *d_seqs, const uint64_t *d_offsets,
+                   const uint32_t *d_lengths, uint32_t n_reads, const gs_params *p,
+                   int fetch_to_host);
+int gs_result_host(gs_ctx *ctx, gs_result_view *out);
+int gs_result_device(gs_ctx *ctx, gs_result_view *out);
+/* Text records exactly as `seed_gen -o` prints them (seed_gen.cu:3625-3647),
+ * appended to an open file descriptor; first_read_no is 1-based. */
+int gs_result_write_text(gs_ctx *ctx, int fd, uint32_t first_read_no, int smem);
+/* Stream the context runs on (a cudaStream_t). */
+void *gs_ctx_stream(gs_ctx *ctx);
+/* Device time (ms) of the last pass's search kernel and of the whole pass,
+ * from CUDA events recorded on the context stream. */
+int gs_ctx_last_timing(gs_ctx *ctx, float *search_ms, float *total_ms);
+
+/* ---- errors ------------------------------------------------------------- */
+const char *gs_last_error(void);
+const char *gs_strerror(int code);
+int gs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

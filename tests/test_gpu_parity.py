@@ -1,0 +1,160 @@
+"""GPU seeding (through the C-ABI) against the CPU oracle, bit for bit.
+
+Every case runs the CUDA path and the oracle on the same index files and the
+same reads and compares, per read, every output seed (begin, end, strand bit,
+SA interval) and every resolved reference position in output order.
+Integer work: the tolerance is zero.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import pyoracle
+from helpers import build_index, pack, random_reference, sample_reads
+
+pytestmark = pytest.mark.gpu
+
+
+def _gs():
+    import gpuseed_gb300 as gs
+    return gs
+
+
+def assert_same(gres, obatch, n_reads, ctx=""):
+    assert gres.n_reads == obatch.n_reads == n_reads
+    for r in range(n_reads):
+        g = gres.read_records(r)
+        o = obatch.read_records(r)
+        assert g == o, f"{ctx} read {r}: gpu {g[:4]} oracle {o[:4]}"
+
+
+@pytest.fixture(scope="module")
+def small(built, tmp_path_factory):
+    d = tmp_path_factory.mktemp("small")
+    codes = random_reference(60_000, 7)
+    prefix = build_index(d, codes, sa_intv=7)
+    gs = _gs()
+    gidx = gs.Index(prefix)
+    oidx = pyoracle.Index(prefix)
+    ctx = gs.Context(gidx)
+    return dict(codes=codes, prefix=prefix, gidx=gidx, oidx=oidx, ctx=ctx, dir=d)
+
+
+def test_kmer_table_matches_oracle(small):
+    g = small["gidx"].kmer_table()
+    o = small["oidx"].kmer_table(13)
+    assert g.shape == o.shape
+    assert np.array_equal(g, o)
+
+
+@pytest.mark.parametrize("kernel", [0, 1], ids=["batched", "plain"])
+@pytest.mark.parametrize("smem", [False, True], ids=["mem", "smem"])
+@pytest.mark.parametrize("n_mode", [0, 1], ids=["nwild", "nstop"])
+def test_random_reads(small, kernel, smem, n_mode):
+    reads = sample_reads(small["codes"], 400, seed=11 + kernel + 2 * n_mode,
+                         lengths=(13, 14, 19, 20, 33, 64, 100, 150, 300))
+    seqs, offs, lens = pack(reads)
+    for k in (13, 19, 20, 31):
+        for lf in (0, 1):
+            gres = small["ctx"].seed(seqs, offs, lens, k=k, smem=smem, n_mode=n_mode, lf_mode=lf,
+                                     kernel=kernel)
+            ob = small["oidx"].seed(seqs, offs, lens, k=k, smem=smem, n_mode=n_mode, lf_mode=lf)
+            assert_same(gres, ob, len(reads), f"k={k} lf={lf}")
+
+
+def test_edge_cases(small):
+    codes = small["codes"]
+    text = "".join("ACGT"[c] for c in codes)
+    sa = pyoracle.suffix_array(codes)
+    primary = small["oidx"].primary
+    q = int(sa[primary + 1])      # text position whose row is primary+1 (LF quirk)
+    reads = [
+        b"",                                   # empty read
+        b"ACGT",                               # shorter than k
+        text[1000:1020].encode(),              # exactly k
+        text[2000:2013].encode(),              # exactly 13 bases
+        b"A" * 80, b"C" * 40 + b"G" * 40,      # homopolymers
+        text[5000:5150].encode(),              # exact forward match
+        text[7000:7100].lower().encode(),      # lowercase letters
+        (text[9000:9030] + "N" + text[9031:9080]).encode(),   # N after the 13-mer
+        (text[9500:9505] + "N" + text[9506:9600]).encode(),   # N inside early 13-mers
+        (text[11000:11050] + "\r").encode(),   # CR kept as a base, as getline gives it
+        b"NNNNNNNNNNNNNNNNNNNNNNNNNNNNNN",
+        text[max(0, q - 60):q + 60].encode(),  # walks through row primary+1
+        text[max(0, q - 3):q + 40].encode(),
+        text[:120].encode(), text[-120:].encode(),
+        b"ACGTRYKMSWBDHV@X" * 4,               # other letters (codes 0 and 5)
+    ]
+    seqs, offs, lens = pack(reads)
+    for kernel in (0, 1):
+        for smem in (False, True):
+            for lf in (0, 1):
+                for k in (13, 20):
+                    gres = small["ctx"].seed(seqs, offs, lens, k=k, smem=smem, lf_mode=lf,
+                                             kernel=kernel)
+                    ob = small["oidx"].seed(seqs, offs, lens, k=k, smem=smem, lf_mode=lf)
+                    assert_same(gres, ob, len(reads), f"edge kernel={kernel} smem={smem} lf={lf} k={k}")
+
+
+def test_empty_batch(small):
+    gres = small["ctx"].seed(b"", np.zeros(0, np.uint64), np.zeros(0, np.uint32), k=20)
+    assert gres.n_reads == 0 and gres.seeds.shape[0] == 0
+
+
+def test_invalid_k(small):
+    gs = _gs()
+    seqs, offs, lens = pack([b"ACGTACGTACGTACGTACGT"])
+    with pytest.raises(gs.GsError) as e:
+        small["ctx"].seed(seqs, offs, lens, k=12)
+    assert e.value.code == -1
+
+
+def test_text_output_identical(small, tmp_path):
+    reads = sample_reads(small["codes"], 300, seed=5, lengths=(50, 100, 150))
+    seqs, offs, lens = pack(reads)
+    for smem in (False, True):
+        small["ctx"].seed(seqs, offs, lens, k=19, smem=smem)
+        gpath = tmp_path / f"g{smem}.txt"
+        with open(gpath, "wb") as f:
+            small["ctx"].write_text(f.fileno(), 1, smem)
+        ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=smem)
+        opath = tmp_path / f"o{smem}.txt"
+        ob.write_text(str(opath), 1, smem)
+        assert gpath.read_bytes() == opath.read_bytes()
+
+
+def test_cli_matches_oracle(small, tmp_path):
+    gs = _gs()
+    reads = sample_reads(small["codes"], 200, seed=9, lengths=(40, 100))
+    fa = tmp_path / "reads.fa"
+    with open(fa, "wb") as f:
+        for i, r in enumerate(reads):
+            f.write(b">r%d\n%s\n" % (i, r))
+    seqs, offs, lens = pack(reads)
+    for smem in (False, True):
+        args = [gs.CLI_PATH, "-k", "19"] + (["-s"] if smem else []) + ["-o", small["prefix"], str(fa)]
+        out = subprocess.run(args, capture_output=True, check=True).stdout
+        ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=smem)
+        opath = tmp_path / "o.txt"
+        ob.write_text(str(opath), 1, smem)
+        assert out == opath.read_bytes()
+
+
+def test_config1_full(built, tmp_path_factory):
+    """BASELINE config 1 at full size: 1 Mbp, 10,000 x 100 bp, k=20, MEM."""
+    gs = _gs()
+    from gpuseed_gb300 import workloads as W
+    d = tmp_path_factory.mktemp("cfg1")
+    codes, nmask = W.make_reference(W.ref_spec(1))
+    prefix = build_index(d, codes, sa_intv=7)
+    seqs, offs, lens = W.make_reads(codes, nmask, W.read_spec(1))
+    gidx = gs.Index(prefix)
+    ctx = gs.Context(gidx)
+    oidx = pyoracle.Index(prefix)
+    ob = oidx.seed(seqs, offs, lens, k=20, smem=False)
+    for kernel in (0, 1):
+        gres = ctx.seed(seqs, offs, lens, k=20, smem=False, kernel=kernel)
+        assert_same(gres, ob, lens.size, f"cfg1 kernel={kernel}")
+    assert ob.seeds.shape[0] > 10_000
