@@ -25,10 +25,11 @@ GS_ERRORS = {-1: "EINVAL", -2: "EIO", -3: "EFORMAT", -4: "ENOMEM", -5: "ECUDA", 
              -7: "EOVERFLOW", -8: "ETIMEOUT", -9: "ESTATE"}
 
 # Every symbol include/gpuseed.h declares.
-EXPORTS = ["gs_index_load", "gs_index_from_host", "gs_index_free", "gs_index_get_info",
+EXPORTS = ["gs_index_load", "gs_index_from_host", "gs_index_build", "gs_index_free", "gs_index_get_info",
            "gs_index_kmer_table", "gs_index_set_l2_window", "gs_ctx_create", "gs_ctx_free",
            "gs_seed", "gs_seed_device", "gs_result_host", "gs_result_device",
-           "gs_result_write_text", "gs_ctx_stream", "gs_ctx_last_timing", "gs_last_error",
+           "gs_result_write_text", "gs_ctx_stream", "gs_ctx_last_timing", "gs_ctx_last_work",
+           "gs_last_error",
            "gs_strerror", "gs_version"]
 
 
@@ -41,7 +42,7 @@ class GsError(RuntimeError):
 class Params(C.Structure):
     _fields_ = [("k", C.c_int32), ("smem", C.c_int32), ("n_mode", C.c_int32),
                 ("lf_mode", C.c_int32), ("kernel", C.c_int32), ("queue_chunk", C.c_int32),
-                ("ctas_per_sm", C.c_int32), ("reserved", C.c_int32)]
+                ("ctas_per_sm", C.c_int32), ("count_work", C.c_int32)]
 
 
 class SeedRec(C.Structure):
@@ -76,6 +77,7 @@ def lib():
         vp, u32, u64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
         L.gs_index_load.argtypes = [C.c_char_p, i32, C.POINTER(vp)]
         L.gs_index_from_host.argtypes = [u32, vp, vp, u64, u32, vp, u64, i32, C.POINTER(vp)]
+        L.gs_index_build.argtypes = [vp, u64, u32, i32, C.c_char_p, C.POINTER(vp)]
         L.gs_index_free.argtypes = [vp]
         L.gs_index_get_info.argtypes = [vp, C.POINTER(IndexInfo)]
         L.gs_index_kmer_table.argtypes = [vp, u64, u64, vp]
@@ -90,6 +92,7 @@ def lib():
         L.gs_ctx_stream.argtypes = [vp]
         L.gs_ctx_stream.restype = vp
         L.gs_ctx_last_timing.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.gs_ctx_last_work.argtypes = [vp, vp]
         L.gs_last_error.restype = C.c_char_p
         L.gs_strerror.restype = C.c_char_p
         L.gs_strerror.argtypes = [i32]
@@ -146,6 +149,21 @@ class Index:
         check(lib().gs_index_set_l2_window(self.h, hit_ratio))
 
 
+def build_index(codes, sa_intv: int = 7, prefix: str | None = None, device: int = 0,
+                load: bool = True):
+    """Builds the .bwt/.sa index of a forward-strand text (codes 0..3) on the GPU;
+    writes the files when `prefix` is given and returns the loaded Index when `load`."""
+    codes = np.ascontiguousarray(codes, dtype=np.uint8)
+    h = C.c_void_p()
+    check(lib().gs_index_build(_ptr(codes), codes.size, sa_intv, device,
+                               prefix.encode() if prefix else None, C.byref(h) if load else None))
+    if not load:
+        return None
+    idx = Index.__new__(Index)
+    idx.h = h
+    return idx
+
+
 class Result:
     """Host copy of one batch's seeds in output order."""
 
@@ -191,8 +209,9 @@ class Context:
 
     @staticmethod
     def params(k=20, smem=False, n_mode=N_WILDCARD, lf_mode=LF_GPUSEED, kernel=KERNEL_BATCHED,
-               queue_chunk=0, ctas_per_sm=0) -> Params:
-        return Params(k, 1 if smem else 0, n_mode, lf_mode, kernel, queue_chunk, ctas_per_sm, 0)
+               queue_chunk=0, ctas_per_sm=0, count_work=False) -> Params:
+        return Params(k, 1 if smem else 0, n_mode, lf_mode, kernel, queue_chunk, ctas_per_sm,
+                      1 if count_work else 0)
 
     def seed(self, seqs, offsets, lengths, **kw) -> Result:
         """Reads in host memory; returns the host result."""
@@ -228,6 +247,12 @@ class Context:
 
     def stream(self) -> int:
         return lib().gs_ctx_stream(self.h) or 0
+
+    def last_work(self):
+        """{n_kmer, n_occ_blocks, n_lf, n_sa} of the last count_work pass."""
+        a = np.zeros(4, dtype=np.uint64)
+        check(lib().gs_ctx_last_work(self.h, _ptr(a)))
+        return dict(n_kmer=int(a[0]), n_occ_blocks=int(a[1]), n_lf=int(a[2]), n_sa=int(a[3]))
 
     def last_timing(self):
         a, b = C.c_float(), C.c_float()

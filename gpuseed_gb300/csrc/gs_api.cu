@@ -131,6 +131,8 @@ struct gs_ctx {
     uint32_t *pmap; size_t cap_pmap;
     uint32_t *queue;
     uint64_t *d_max;
+    unsigned long long *d_work;
+    uint64_t work[4];
     void *cub_tmp; size_t cap_cub;
     uint64_t *h_small;          /* pinned scalars */
     /* host result */
@@ -165,6 +167,7 @@ extern "C" int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out)
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
     if (e == cudaSuccess) e = cudaMalloc(&c->queue, 16);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_max, 16);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_work, 32);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_small, 64);
     if (e != cudaSuccess) {
         int rc = gs_cuda_fail(e, "gs_ctx_create");
@@ -205,6 +208,7 @@ extern "C" void gs_ctx_free(gs_ctx *c)
     cudaFree(c->seed_off); cudaFree(c->pos_off);
     cudaFree(c->slots); cudaFree(c->hist); cudaFree(c->seeds); cudaFree(c->seed_pos);
     cudaFree(c->pos); cudaFree(c->pmap); cudaFree(c->queue); cudaFree(c->d_max);
+    cudaFree(c->d_work);
     cudaFree(c->cub_tmp);
     cudaFreeHost(c->h_small);
     cudaFreeHost(c->h_seed_off); cudaFreeHost(c->h_pos_off);
@@ -218,6 +222,13 @@ extern "C" void gs_ctx_free(gs_ctx *c)
 }
 
 extern "C" void *gs_ctx_stream(gs_ctx *c) { return c ? (void *)c->st : NULL; }
+
+extern "C" int gs_ctx_last_work(gs_ctx *c, uint64_t out[4])
+{
+    if (!c || !out) return GS_EINVAL;
+    memcpy(out, c->work, sizeof(c->work));
+    return GS_OK;
+}
 
 extern "C" int gs_ctx_last_timing(gs_ctx *c, float *search_ms, float *total_ms)
 {
@@ -309,8 +320,11 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     B.n_mode = p->n_mode;
     B.lf_mode = p->lf_mode;
     B.queue = c->queue;
+    B.work = p->count_work ? c->d_work : NULL;
+    memset(c->work, 0, sizeof(c->work));
 
     GS_CUDA(cudaEventRecord(c->ev0, st));
+    if (B.work) GS_CUDA(cudaMemsetAsync(c->d_work, 0, 32, st));
     GS_CUDA(cudaMemsetAsync(c->queue, 0, 16, st));
     B.slot_off = c->slot_cnt;
     B.item_off = c->item_cnt;
@@ -375,6 +389,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     RC(gs_launch_locate(I, B, n_seeds, n_pos, st));
     GS_CUDA(cudaEventRecord(c->ev1, st));
     GS_CUDA(cudaMemcpyAsync(&c->h_small[5], c->queue + 1, 4, cudaMemcpyDeviceToHost, st));
+    if (B.work) GS_CUDA(cudaMemcpyAsync(&c->h_small[6], c->d_work, 32, cudaMemcpyDeviceToHost, st));
     c->n_seeds = n_seeds;
     c->n_pos = n_pos;
     if (fetch) {
@@ -392,6 +407,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     }
     GS_CUDA(cudaStreamSynchronize(st));
     uint32_t flags = (uint32_t)(c->h_small[5] & 0xffffffffu);
+    if (B.work) memcpy(c->work, &c->h_small[6], sizeof(c->work));
     cudaEventElapsedTime(&c->t_search, c->ev_s0, c->ev_s1);
     cudaEventElapsedTime(&c->t_total, c->ev0, c->ev1);
     if (flags & GS_FLAG_WALK) {

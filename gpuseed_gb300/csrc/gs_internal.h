@@ -55,6 +55,7 @@ struct GsBatch {
     uint32_t *pmap;            /* position -> seed */
     uint64_t seed_cap, pos_cap;
     uint32_t *queue;           /* [0]: work-queue head, [1]: status flags */
+    unsigned long long *work;  /* NULL or [kmer, occ blocks, lf steps, sa samples] */
 };
 
 #define GS_FLAG_WALK 1u

@@ -192,27 +192,46 @@ __global__ void __launch_bounds__(256) gs_expand(const uint64_t *seed_pos, const
 __global__ void __launch_bounds__(256) gs_locate(GsDevIndex I, const gs_seed_rec *seeds,
                                                  const uint64_t *seed_pos, const uint32_t *pmap,
                                                  uint64_t n_pos, uint32_t *out, int lf_mode,
-                                                 uint32_t *flags)
+                                                 uint32_t *flags, unsigned long long *work)
 {
-    uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n_pos) return;
-    uint32_t s = pmap[j];
-    gs_seed_rec S = seeds[s];
-    uint32_t row = S.l + (uint32_t)(j - seed_pos[s]);
-    if (S.xl <= S.xu && row >= S.xl) row += S.xu - S.xl + 1u;
-    /* locate_seeds_gpu (:668-684): LF until a sampled row; a consistent
-     * index reaches one within seq_len+1 steps */
+    const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t steps = 0;
-    const uint32_t cap = I.seq_len + 2u;
-    while (row % I.sa_intv) {
-        row = gs_lf(I, row, lf_mode);
-        if (++steps > cap) {
+    const bool active = j < n_pos;
+    if (active) {
+        uint32_t s = pmap[j];
+        gs_seed_rec S = seeds[s];
+        uint32_t row = S.l + (uint32_t)(j - seed_pos[s]);
+        if (S.xl <= S.xu && row >= S.xl) row += S.xu - S.xl + 1u;
+        /* locate_seeds_gpu (:668-684): LF until a sampled row; a consistent
+         * index reaches one within seq_len+1 steps */
+        const uint32_t cap = I.seq_len + 2u;
+        bool bad = false;
+        while (row % I.sa_intv) {
+            row = gs_lf(I, row, lf_mode);
+            if (++steps > cap) {
+                bad = true;
+                break;
+            }
+        }
+        if (bad) {
             atomicOr(flags, GS_FLAG_WALK);
             out[j] = 0xffffffffu;
-            return;
+        } else {
+            out[j] = __ldg(&I.sa[row / I.sa_intv]) + steps;
         }
     }
-    out[j] = __ldg(&I.sa[row / I.sa_intv]) + steps;
+    if (work) {
+        /* every lane of the block reaches here: one atomic per warp */
+        unsigned long long st = steps, np = active ? 1ull : 0ull;
+        for (int off = 16; off; off >>= 1) {
+            st += __shfl_xor_sync(0xffffffffu, st, off);
+            np += __shfl_xor_sync(0xffffffffu, np, off);
+        }
+        if ((threadIdx.x & 31) == 0 && np) {
+            atomicAdd(&work[2], st);
+            atomicAdd(&work[3], np);
+        }
+    }
 }
 
 int gs_launch_finalize_count(const GsDevIndex &I, GsBatch &B, cudaStream_t st)
@@ -244,7 +263,7 @@ int gs_launch_locate(const GsDevIndex &I, GsBatch &B, uint64_t n_seeds, uint64_t
     GS_CUDA(cudaGetLastError());
     gs_locate<<<(unsigned)((n_pos + 255) / 256), 256, 0, st>>>(I, B.seeds, B.seed_pos, B.pmap,
                                                                 n_pos, B.pos, B.lf_mode,
-                                                                B.queue + 1);
+                                                                B.queue + 1, B.work);
     GS_CUDA(cudaGetLastError());
     return GS_OK;
 }

@@ -235,6 +235,7 @@ __global__ void __launch_bounds__(128) gs_search_plain(GsDevIndex I, GsBatch B)
     uint32_t *H = B.hist + B.offsets[r];
     GsRec *slots = B.slots + B.slot_off[r];
     const int iL = (int)L;
+    unsigned long long w_kmer = 0, w_blk = 0;
 
     for (int strand = 0; strand < 2; strand++) {
         const bool fwd = strand == 0;
@@ -254,6 +255,7 @@ __global__ void __launch_bounds__(128) gs_search_plain(GsDevIndex I, GsBatch B)
                 uint2 iv = __ldg(&I.kmer[pat]);
                 l = iv.x;
                 u = iv.y;
+                w_kmer++;
             }
             int pos = fwd ? anchor - (GS_K0 - 1) : anchor + (GS_K0 - 1);
             bool killed = false;
@@ -271,7 +273,7 @@ __global__ void __launch_bounds__(128) gs_search_plain(GsDevIndex I, GsBatch B)
                     if (c > 3u) {
                         if (NSTOP) break;
                     } else {
-                        gs_step(I, nl, nu, c);
+                        w_blk += (unsigned long long)gs_step(I, nl, nu, c);
                         if (nl > nu) break;
                     }
                     l = nl;
@@ -296,6 +298,10 @@ __global__ void __launch_bounds__(128) gs_search_plain(GsDevIndex I, GsBatch B)
             uint64_t slot = fwd ? (uint64_t)(anchor - (k - 1)) : (uint64_t)n + (uint64_t)anchor;
             slots[slot] = rec;
         }
+    }
+    if (B.work) {
+        atomicAdd(&B.work[0], w_kmer);
+        atomicAdd(&B.work[1], w_blk);
     }
 }
 

@@ -56,7 +56,7 @@ typedef struct {
     int32_t kernel;     /* GS_KERNEL_BATCHED | GS_KERNEL_PLAIN */
     int32_t queue_chunk;    /* work items a warp takes per queue grab (0 = auto) */
     int32_t ctas_per_sm;    /* persistent CTAs per SM (0 = auto) */
-    int32_t reserved;
+    int32_t count_work;     /* 1: count algorithmic work (plain kernel walk + locate) */
 } gs_params;
 
 /* One output seed, in output order.  x/y are the reference's int2 read
@@ -102,6 +102,14 @@ int gs_index_get_info(const gs_index *idx, gs_index_info *out);
 /* Copies the device 13-mer table (2*4^13 uint32: l,u per pattern) or a
  * range of it to host memory (pre_calc_seed_intervals_gpu, seed_gen.cu:2648). */
 int gs_index_kmer_table(const gs_index *idx, uint64_t first, uint64_t count, uint32_t *out);
+/* Index construction, replacing build_index.sh (bwa index -b sa -r R and
+ * bwa index -b bwt, build_index.sh:36-75): suffix array of the forward-strand
+ * text on the GPU, BWT, 64-row occurrence blocks and the row-sampled SA, in
+ * the file layout seed_gen.cu:2685-2736 reads.  codes: n bytes in 0..3.
+ * Writes <prefix>.bwt and <prefix>.sa when prefix is not NULL; loads the
+ * index on `device` into *out when out is not NULL. */
+int gs_index_build(const uint8_t *codes, uint64_t n, uint32_t sa_intv, int device,
+                   const char *prefix, gs_index **out);
 /* Keeps the occurrence table in L2 under an access-policy window on every
  * context stream (fraction of the set-aside, 0 disables). */
 int gs_index_set_l2_window(gs_index *idx, float hit_ratio);
@@ -131,6 +139,10 @@ void *gs_ctx_stream(gs_ctx *ctx);
 /* Device time (ms) of the last pass's search kernel and of the whole pass,
  * from CUDA events recorded on the context stream. */
 int gs_ctx_last_timing(gs_ctx *ctx, float *search_ms, float *total_ms);
+/* Algorithmic work of the last pass run with count_work = 1 and the plain
+ * kernel: 13-mer table lookups, 32-byte occurrence blocks of the
+ * containment-stopped walk, LF steps and SA samples of the locate stage. */
+int gs_ctx_last_work(gs_ctx *ctx, uint64_t out[4]);
 
 /* ---- errors ------------------------------------------------------------- */
 const char *gs_last_error(void);

@@ -158,3 +158,18 @@ def test_config1_full(built, tmp_path_factory):
         gres = ctx.seed(seqs, offs, lens, k=20, smem=False, kernel=kernel)
         assert_same(gres, ob, lens.size, f"cfg1 kernel={kernel}")
     assert ob.seeds.shape[0] > 10_000
+
+
+def test_work_counters_match_oracle(small):
+    """The plain kernel's containment-stopped walk does exactly the oracle's
+    canonical work (13-mer lookups, occurrence blocks, LF steps, SA samples)."""
+    reads = sample_reads(small["codes"], 300, seed=21, lengths=(50, 100, 150, 250))
+    seqs, offs, lens = pack(reads)
+    for smem in (False, True):
+        small["ctx"].seed(seqs, offs, lens, k=19, smem=smem, kernel=1, count_work=True)
+        w = small["ctx"].last_work()
+        ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=smem, pruned=True)
+        assert w["n_kmer"] == ob.work["n_kmer"]
+        assert w["n_occ_blocks"] == ob.work["n_occ_blocks"]
+        assert w["n_lf"] == ob.work["n_lf"]
+        assert w["n_sa"] == ob.work["n_sa"]
