@@ -1,0 +1,451 @@
+"""Seeding benchmark: reads/s of the batched GPU pipeline vs the plain kernel.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config 3] [--reads R] [--ref-len L]
+
+Workload (default): the human-scale configuration the metric is quoted on --
+a 3.1 Gbp synthetic reference (41% GC, segmental duplications, diverged
+300 bp repeat families up to 45% repeats, 1% N blocks), index with SA ratio 7
+built on the GPU, 10M reads of 50/75/100/150/250 bp with 1% substitutions and
+0.05% indels, k = 19, SMEM mode.  Data is synthetic and seeded.
+
+One step = one pass of the whole pipeline (search, filters, ordering, SA
+walk) over all reads, inputs resident in HBM.  The inputs (1.25 GB of reads)
+and the index (3.8 GB) are larger than L2, so no flush is needed between
+steps.  `e2e` is the same pass through the C-ABI with host buffers: pinned
+host -> device copies of the reads and device -> host copies of every seed and
+position inside the timed region.
+
+--impl reference times the reference's seeding semantics on the host cores:
+the CPU restatement (oracle/, a "port") with every host thread, on a bounded
+sample of the same reads per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "reads/sec SMEM (bit-exact) batched vs plain kernel on 1 GB300; p50/p99 latency"
+CACHE = os.environ.get("GPUSEED_BENCH_CACHE", "/tmp/gpuseed_bench_cache")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# --------------------------------------------------------------------------
+# workload
+
+def workload(cfg, ref_len, n_reads, rank=0, load_gpu_index=True):
+    """Reference + index files (built on the GPU, cached per box) + reads of this rank."""
+    from gpuseed_gb300 import workloads as W
+    spec = W.ref_spec(cfg, ref_len)
+    rspec = W.read_spec(cfg, n_reads)
+    rspec.seed += 7919 * rank
+    tag = f"cfg{cfg}_L{spec.length}"
+    d = os.path.join(CACHE, tag)
+    os.makedirs(d, exist_ok=True)
+    prefix = os.path.join(d, "ref")
+    t0 = time.time()
+    codes, nmask = W.make_reference(spec)
+    log(f"[bench] reference {spec.length:,} bp generated in {time.time() - t0:.1f}s")
+    idx = None
+    import gpuseed_gb300 as gs
+    from gpuseed_gb300 import build as gbuild
+    gbuild.build()
+    t0 = time.time()
+    if os.path.exists(prefix + ".sa") and os.path.exists(prefix + ".bwt"):
+        if load_gpu_index:
+            idx = gs.Index(prefix)
+        log(f"[bench] index files from cache, loaded in {time.time() - t0:.1f}s")
+    else:
+        idx = gs.build_index(codes, 7, prefix=prefix + ".tmp", load=load_gpu_index)
+        for ext in (".bwt", ".sa"):
+            os.replace(prefix + ".tmp" + ext, prefix + ext)
+        log(f"[bench] index built on GPU in {time.time() - t0:.1f}s")
+    t0 = time.time()
+    seqs, offs, lens = W.make_reads(codes, nmask, rspec)
+    log(f"[bench] {lens.size:,} reads ({int(lens.sum()):,} bases) in {time.time() - t0:.1f}s")
+    del codes, nmask
+    return dict(prefix=prefix, idx=idx, seqs=seqs, offs=offs, lens=lens, k=W.CONFIG_K[cfg],
+                smem=W.CONFIG_SMEM[cfg], spec=spec)
+
+
+# --------------------------------------------------------------------------
+# clocks (nvidia-smi sampled during the timed region)
+
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if len(s) > 8 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) > 8 and s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for i, n in enumerate(names):
+                if len(s) > 5 + i and s[5 + i].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.samples)}
+
+
+# --------------------------------------------------------------------------
+# distributed helpers (one process per GPU, reads sharded by rank)
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws, backend):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def max_over_ranks(dist, value, device=None):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, value, device=None):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# --------------------------------------------------------------------------
+# CPU baseline (oracle port, all host threads, bounded sample)
+
+def cpu_baseline(prefix, seqs, offs, lens, k, smem, table, target_s=12.0, threads=0):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build()
+    oidx = pyoracle.Index(prefix)
+    threads = threads or len(os.sched_getaffinity(0))
+    n_total = lens.size
+
+    def run(n):
+        t0 = time.perf_counter()
+        oidx.seed(seqs, offs[:n], lens[:n], k=k, smem=smem, pruned=True, threads=threads,
+                  table=table)
+        return time.perf_counter() - t0
+
+    n = min(20_000, n_total)
+    dt = run(n)
+    n2 = int(min(n_total, max(n, n / max(dt, 1e-3) * target_s)))
+    if n2 > n:
+        dt = run(n2)
+        n = n2
+    return {"value": n / dt, "unit": "reads/s", "cores": threads, "kind": "port",
+            "sample": f"first {n:,} reads of the workload, oracle containment-stopped walk, "
+                      f"{threads} threads, {dt:.1f}s"}
+
+
+# --------------------------------------------------------------------------
+
+def run_reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    cfg = args.config
+    w = workload(cfg, args.ref_len, args.reads, load_gpu_index=False)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build()
+    oidx = pyoracle.Index(w["prefix"])
+    threads = len(os.sched_getaffinity(0))
+    t0 = time.time()
+    table = oidx.table13(threads)
+    log(f"[bench] oracle 13-mer table in {time.time() - t0:.1f}s")
+    # size one step's sample to ~args.ref_step_s seconds of CPU work
+    lens, offs, seqs = w["lens"], w["offs"], w["seqs"]
+    n = min(20_000, lens.size)
+    t0 = time.perf_counter()
+    oidx.seed(seqs, offs[:n], lens[:n], k=w["k"], smem=w["smem"], pruned=True, threads=threads,
+              table=table)
+    rate = n / (time.perf_counter() - t0)
+    n_step = int(min(lens.size, max(n, rate * args.ref_step_s)))
+    times = []
+    for s in range(args.warmup + args.steps):
+        lo = (s * n_step) % max(1, lens.size - n_step + 1)
+        t0 = time.perf_counter()
+        oidx.seed(seqs, offs[lo:lo + n_step], lens[lo:lo + n_step], k=w["k"], smem=w["smem"],
+                  pruned=True, threads=threads, table=table)
+        dt = time.perf_counter() - t0
+        if s >= args.warmup:
+            times.append(dt)
+    tot = sum(times)
+    value = n_step * len(times) / tot
+    sample = f"{n_step:,} reads per step (oracle containment-stopped walk, {threads} threads)"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "reads/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * tot / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": config_dict(args, w, sample_note=sample),
+        "cpu_baseline": {"value": value, "unit": "reads/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(args, w, sample_note=None):
+    spec = w["spec"]
+    d = {"workload": f"config {args.config}: {spec.length / 1e9:.2f} Gbp synthetic reference, "
+                     f"{w['lens'].size:,} reads {'SMEM' if w['smem'] else 'MEM'} k={w['k']}",
+         "ref_bp": int(spec.length), "reads": int(w["lens"].size), "bases": int(w["lens"].sum()),
+         "k": w["k"], "mode": "smem" if w["smem"] else "mem", "sa_intv": 7,
+         "l2": "inputs larger than L2 (reads 1.25 GB, index 3.8 GB); no flush"}
+    if sample_note:
+        d["sample"] = sample_note
+    return d
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=3)
+    ap.add_argument("--reads", type=int, default=0)
+    ap.add_argument("--ref-len", type=int, default=0)
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--ref-step-s", type=float, default=8.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+
+    import torch
+    import gpuseed_gb300 as gs
+    from gpuseed_gb300 import build as gbuild
+    gbuild.build()
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = dist_init(ws, "nccl")
+    dev = torch.device("cuda", local)
+
+    w = workload(args.config, args.ref_len, args.reads, rank=rank)
+    idx = w["idx"]
+    seqs, offs, lens = w["seqs"], w["offs"], w["lens"]
+    n_reads = int(lens.size)
+    k, smem = w["k"], w["smem"]
+    ctx = gs.Context(idx)
+    st = torch.cuda.ExternalStream(ctx.stream())
+
+    d_seqs = torch.from_numpy(seqs).to(dev)
+    d_offs = torch.from_numpy(offs.view(np.int64)).to(dev)
+    d_lens = torch.from_numpy(lens.view(np.int32)).to(dev)
+    torch.cuda.synchronize()
+
+    def step(kernel, count=False):
+        ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), n_reads,
+                        fetch=False, k=k, smem=smem, kernel=kernel, count_work=count)
+
+    def timed(kernel, steps, warmup, clocks=None):
+        for _ in range(warmup):
+            step(kernel)
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        search_ms = []
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        cm = clocks if clocks is not None else _Null()
+        with cm:
+            torch.cuda.synchronize()
+            e0.record(st)
+            for _ in range(steps):
+                step(kernel)
+                search_ms.append(ctx.last_timing()[0])
+            e1.record(st)
+            torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        return e0.elapsed_time(e1), search_ms
+
+    # batched (the headline)
+    clocks = Clocks(local)
+    ms, search_ms = timed(gs.KERNEL_BATCHED, args.steps, args.warmup, clocks)
+    ms = max_over_ranks(dist, ms, dev)
+    total_reads = sum_over_ranks(dist, n_reads * args.steps, dev)
+    value = total_reads / (ms / 1e3)
+    n_seeds, n_pos = ctx.device_counts()
+    log(f"[bench] batched: {ms / args.steps:.1f} ms/step, {value:,.0f} reads/s, "
+        f"search {statistics.mean(search_ms):.1f} ms, seeds {n_seeds:,} positions {n_pos:,}")
+
+    # plain one-read-per-thread kernel, same pipeline otherwise
+    pms, psearch = timed(gs.KERNEL_PLAIN, args.plain_steps, 1)
+    pms = max_over_ranks(dist, pms, dev)
+    plain_value = sum_over_ranks(dist, n_reads * args.plain_steps, dev) / (pms / 1e3)
+    log(f"[bench] plain: {pms / args.plain_steps:.1f} ms/step, {plain_value:,.0f} reads/s, "
+        f"search {statistics.mean(psearch):.1f} ms")
+
+    # algorithmic work of the canonical walk, counted on the whole workload
+    step(gs.KERNEL_PLAIN, count=True)
+    torch.cuda.synchronize()
+    work = ctx.last_work()
+    search_bytes = 32 * (work["n_kmer"] + work["n_occ_blocks"])
+    mean_search_s = statistics.mean(search_ms) / 1e3
+    achieved = search_bytes / mean_search_s / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    except Exception:
+        peak, peak_src = 6800.0, "fallback"
+    traffic = None
+    try:
+        tj = json.load(open(os.path.join(ROOT, "profiles", "search_traffic.json")))
+        traffic = float(tj["dram_bytes_per_read"]) * n_reads
+    except Exception:
+        pass
+    # random 32-byte gather roofline on a 16 GB buffer
+    import ctypes as C
+    L = gs.lib()
+    L.gs_probe_random_gather.argtypes = [C.c_int, C.c_uint64, C.c_uint32, C.c_uint64,
+                                         C.POINTER(C.c_double)]
+    g32 = C.c_double()
+    gs.check(L.gs_probe_random_gather(local, 16 << 30, 32, 1 << 30, C.byref(g32)))
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "peak_source": f"{peak_src} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
+                "kernel": "gs_search_batched",
+                "algorithmic_bytes_per_launch": search_bytes,
+                "random_32B_gather_gbs": g32.value,
+                "frac_of_random_32B": achieved / g32.value if g32.value else None}
+    log(f"[bench] search {achieved:.0f} GB/s algorithmic = {achieved / peak:.3f} of {peak:.0f} GB/s; "
+        f"random 32B gather {g32.value:.0f} GB/s")
+
+    # e2e through the C-ABI with pinned host buffers
+    h_seqs = torch.from_numpy(seqs).pin_memory()
+    h_offs = torch.from_numpy(offs.view(np.int64)).pin_memory()
+    h_lens = torch.from_numpy(lens.view(np.int32)).pin_memory()
+    hs = h_seqs.numpy().view(np.uint8)
+    ho = h_offs.numpy().view(np.uint64)
+    hl = h_lens.numpy().view(np.uint32)
+    p = ctx.params(k=k, smem=smem)
+    import ctypes as C2
+    for _ in range(2):
+        gs.check(L.gs_seed(ctx.h, C2.c_void_p(hs.ctypes.data), C2.c_void_p(ho.ctypes.data),
+                           C2.c_void_p(hl.ctypes.data), n_reads, C2.byref(p)))
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    e2e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        gs.check(L.gs_seed(ctx.h, C2.c_void_p(hs.ctypes.data), C2.c_void_p(ho.ctypes.data),
+                           C2.c_void_p(hl.ctypes.data), n_reads, C2.byref(p)))
+    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(dist, e2e_s, dev)
+    e2e_value = sum_over_ranks(dist, n_reads * e2e_steps, dev) / e2e_s
+    res = ctx.result()
+    h2d = int(seqs.nbytes + offs.nbytes + lens.nbytes)
+    d2h = int(res.seeds.nbytes + res.pos.nbytes + res.read_seed_off.nbytes + res.read_pos_off.nbytes)
+    log(f"[bench] e2e: {e2e_value:,.0f} reads/s")
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        table = idx.kmer_table()
+        cpu = cpu_baseline(w["prefix"], seqs, offs, lens, k, smem, table)
+        log(f"[bench] cpu baseline: {cpu['value']:,.0f} reads/s on {cpu['cores']} threads")
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": config_dict(args, w),
+            "plain": {"value": plain_value, "unit": "reads/s", "ms_per_step": pms / args.plain_steps,
+                      "search_ms": statistics.mean(psearch)},
+            "batched_over_plain": value / plain_value,
+            "search_ms": statistics.mean(search_ms),
+            "seeds_per_step": n_seeds, "positions_per_step": n_pos,
+            "work": work,
+            "e2e": {"value": e2e_value, "unit": "reads/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": 6 * args.steps,
+            "clocks": clocks.summary(),
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "latency": None,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,84 @@
+/*
+ * gs_tools.cu -- measurement probes (no counterpart in the reference).
+ *
+ * gs_probe_random_gather: the random-sector roofline of the seeding path.
+ * Every occurrence lookup of the search is one 32-byte block at an
+ * unpredictable address; this probe issues independent 32- or 64-byte
+ * vector loads at uniformly random aligned addresses of a buffer larger than
+ * L2 and reports the loaded bytes per second (CUDA events, after warm-up).
+ */
+#include "gs_internal.h"
+
+static __device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+template <int WORDS>
+static __global__ void __launch_bounds__(256) gather_kernel(const uint32_t *__restrict__ buf,
+                                                            uint64_t n_blocks, uint64_t per_thread,
+                                                            uint64_t salt, uint32_t *sink)
+{
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t acc = 0;
+    for (uint64_t i = 0; i < per_thread; i++) {
+        uint64_t h = mix64(salt + tid * per_thread + i);
+        uint64_t blk = (uint64_t)(((unsigned __int128)h * n_blocks) >> 64);
+        const uint32_t *p = buf + blk * WORDS;
+        uint32_t a0, a1, a2, a3, a4, a5, a6, a7;
+        asm volatile("ld.global.nc.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                     : "=r"(a0), "=r"(a1), "=r"(a2), "=r"(a3), "=r"(a4), "=r"(a5), "=r"(a6), "=r"(a7)
+                     : "l"(p));
+        acc ^= a0 ^ a1 ^ a2 ^ a3 ^ a4 ^ a5 ^ a6 ^ a7;
+        if (WORDS == 16) {
+            asm volatile("ld.global.nc.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                         : "=r"(a0), "=r"(a1), "=r"(a2), "=r"(a3), "=r"(a4), "=r"(a5), "=r"(a6), "=r"(a7)
+                         : "l"(p + 8));
+            acc ^= a0 ^ a1 ^ a2 ^ a3 ^ a4 ^ a5 ^ a6 ^ a7;
+        }
+    }
+    if (acc == 0x9e3779b9u) sink[0] = acc;   /* keeps the loads alive */
+}
+
+extern "C" int gs_probe_random_gather(int device, uint64_t bytes, uint32_t load_bytes,
+                                      uint64_t n_loads, double *gbps)
+{
+    if (!gbps || (load_bytes != 32 && load_bytes != 64) || bytes < 1024 || n_loads == 0) {
+        gs_set_error("gs_probe_random_gather: load_bytes 32|64, bytes >= 1024, n_loads > 0");
+        return GS_EINVAL;
+    }
+    GS_CUDA(cudaSetDevice(device));
+    int sms = 0;
+    GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    uint32_t *buf = NULL, *sink = NULL;
+    GS_CUDA(cudaMalloc(&buf, bytes));
+    cudaError_t e = cudaMalloc(&sink, 4);
+    cudaEvent_t a = NULL, b = NULL;
+    if (e == cudaSuccess) e = cudaMemset(buf, 1, bytes);
+    if (e == cudaSuccess) e = cudaEventCreate(&a);
+    if (e == cudaSuccess) e = cudaEventCreate(&b);
+    uint64_t n_blocks = bytes / load_bytes;
+    uint32_t grid = (uint32_t)sms * 8;
+    uint64_t threads = (uint64_t)grid * 256;
+    uint64_t per = (n_loads + threads - 1) / threads;
+    float best = 1e30f;
+    for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {
+        cudaEventRecord(a);
+        if (load_bytes == 32) gather_kernel<8><<<grid, 256>>>(buf, n_blocks, per, 0x1234 + rep * 77, sink);
+        else gather_kernel<16><<<grid, 256>>>(buf, n_blocks, per, 0x1234 + rep * 77, sink);
+        cudaEventRecord(b);
+        e = cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        if (rep > 0 && ms < best) best = ms;   /* first launch is warm-up */
+    }
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    cudaFree(buf);
+    cudaFree(sink);
+    if (e != cudaSuccess) return gs_cuda_fail(e, "random gather probe");
+    *gbps = (double)(per * threads) * load_bytes / (best * 1e-3) / 1e9;
+    return GS_OK;
+}

@@ -1,0 +1,24 @@
+/*
+ * gpuseed_tools.h -- measurement probes of libgpuseed.so.  No counterpart in
+ * the reference: they measure the hardware the seeding path runs on.
+ */
+#ifndef GPUSEED_TOOLS_H
+#define GPUSEED_TOOLS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Random-gather roofline: n_loads independent loads of load_bytes (32 or 64)
+ * at uniformly random aligned addresses of a device buffer of `bytes` bytes
+ * (choose bytes > L2).  *gbps = loaded bytes per second / 1e9, best of three
+ * timed launches after one warm-up launch. */
+int gs_probe_random_gather(int device, uint64_t bytes, uint32_t load_bytes, uint64_t n_loads,
+                           double *gbps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -152,14 +152,15 @@ class Index:
         return self._table
 
     def seed(self, seqs: bytes, offsets, lengths, k=20, smem=False, n_mode=N_WILDCARD,
-             lf_mode=LF_GPUSEED, pruned=False, threads=0, use_table=False) -> "Batch":
+             lf_mode=LF_GPUSEED, pruned=False, threads=0, use_table=False, table=None) -> "Batch":
         offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
         lengths = np.ascontiguousarray(lengths, dtype=np.uint32)
         buf = np.frombuffer(seqs, dtype=np.uint8) if isinstance(seqs, (bytes, bytearray)) else seqs
         buf = np.ascontiguousarray(buf, dtype=np.uint8)
         p = _Params(k, 1 if smem else 0, n_mode, lf_mode)
         out = C.POINTER(_Batch)()
-        table = self.table13(threads) if use_table else None
+        if table is None and use_table:
+            table = self.table13(threads)
         rc = lib().or_seed_batch(self.h, _ptr(table), _ptr(buf), _ptr(offsets), _ptr(lengths),
                                  lengths.size, C.byref(p), 1 if pruned else 0, threads,
                                  C.byref(out))
