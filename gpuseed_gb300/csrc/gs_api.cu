@@ -168,7 +168,7 @@ extern "C" int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out)
     if (e == cudaSuccess) e = cudaMalloc(&c->queue, 16);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_max, 16);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_work, 32);
-    if (e == cudaSuccess) e = cudaMallocHost(&c->h_small, 64);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_small, 256);
     if (e != cudaSuccess) {
         int rc = gs_cuda_fail(e, "gs_ctx_create");
         gs_ctx_free(c);
