@@ -609,6 +609,7 @@ typedef struct {
     uint64_t *read_seed_start, *read_pos_start;
     uint32_t *read_n_seeds;
     uint64_t *read_n_pos;
+    uint32_t *read_n_fwd;
 } batch_ctx;
 
 typedef struct {
@@ -669,6 +670,7 @@ static void *seed_worker(void *arg)
                                       hist, c->pruned))
                         rv[nr++] = rec;
                 }
+                c->read_n_fwd[r] = (uint32_t)nf;
                 int rc = finish_read(c->idx, c->p, fw, nf, rv, nr, t, &ns);
                 if (rc) { t->status = rc; break; }
             }
@@ -699,6 +701,7 @@ int or_seed_batch(const or_index *idx, const uint32_t *table13,
     c.read_pos_start = (uint64_t *)calloc(n_reads + 1, 8);
     c.read_n_seeds = (uint32_t *)calloc(n_reads + 1, 4);
     c.read_n_pos = (uint64_t *)calloc(n_reads + 1, 8);
+    c.read_n_fwd = (uint32_t *)calloc(n_reads + 1, 4);
     worker_arg *wa = (worker_arg *)calloc((size_t)n_threads, sizeof(worker_arg));
     pthread_t *th = (pthread_t *)calloc((size_t)n_threads, sizeof(pthread_t));
     or_batch *bt = (or_batch *)calloc(1, sizeof(or_batch));
@@ -717,6 +720,7 @@ int or_seed_batch(const or_index *idx, const uint32_t *table13,
     /* gather per-thread buffers in read order */
     bt->n_reads = n_reads;
     bt->read_n_seeds = c.read_n_seeds; c.read_n_seeds = NULL;
+    bt->read_n_fwd = c.read_n_fwd; c.read_n_fwd = NULL;
     bt->read_seed_off = (uint64_t *)calloc(n_reads + 1, 8);
     bt->read_pos_off = (uint64_t *)calloc(n_reads + 1, 8);
     if (!bt->read_seed_off || !bt->read_pos_off) { rc = OR_ENOMEM; goto done; }
@@ -747,7 +751,7 @@ done:
     if (wa) for (int t = 0; t < n_threads; t++) { free(wa[t].tb.seeds); free(wa[t].tb.pos); }
     free(wa); free(th);
     free(c.read_thread); free(c.read_seed_start); free(c.read_pos_start);
-    free(c.read_n_seeds); free(c.read_n_pos);
+    free(c.read_n_seeds); free(c.read_n_pos); free(c.read_n_fwd);
     if (rc) { or_batch_free(bt); return rc; }
     *out = bt;
     return OR_OK;
@@ -756,7 +760,7 @@ done:
 void or_batch_free(or_batch *b)
 {
     if (!b) return;
-    free(b->read_n_seeds); free(b->read_seed_off); free(b->read_pos_off);
+    free(b->read_n_seeds); free(b->read_seed_off); free(b->read_pos_off); free(b->read_n_fwd);
     free(b->seeds); free(b->pos);
     free(b);
 }

@@ -9,7 +9,7 @@
  * Every function restates one piece of the reference (nahmedraja/GPUseed,
  * single file seed_gen.cu) and cites the lines it follows.  The reference has
  * no tests, fixtures or golden vectors; the restatement is pinned by
- *   (1) a brute-force substring matcher (tests/test_oracle_bruteforce.py),
+ *   (1) a brute-force substring matcher (tests/bruteforce.py, tests/golden/),
  *   (2) a CPU build of the reference's own kernel bodies
  *       (oracle/ref_emul/, built into oracle/_ref/ from the reference tree
  *       when it is present), compared on seeded inputs.
@@ -79,6 +79,10 @@ typedef struct {
     /* algorithmic work counters (32-byte units), summed over reads */
     uint64_t n_kmer, n_occ_blocks, n_lf, n_sa, n_steps;
     int32_t status;            /* 0 or negative error */
+    uint32_t *read_n_fwd;      /* per read: forward records before the filters
+                                  (full walk only; the reference's MEM filter
+                                  leaves the single record of a read with
+                                  exactly one unwritten, seed_gen.cu:1110) */
 } or_batch;
 
 /* ---- index ---------------------------------------------------------- */

@@ -39,7 +39,8 @@ class _Batch(C.Structure):
                 ("pos", C.POINTER(C.c_uint32)),
                 ("n_kmer", C.c_uint64), ("n_occ_blocks", C.c_uint64), ("n_lf", C.c_uint64),
                 ("n_sa", C.c_uint64), ("n_steps", C.c_uint64),
-                ("status", C.c_int32)]
+                ("status", C.c_int32),
+                ("read_n_fwd", C.POINTER(C.c_uint32))]
 
 
 def build():
@@ -186,6 +187,7 @@ class Batch:
         else:
             self.seeds = np.zeros((0, 5), np.uint32)
         self.pos = np.ctypeslib.as_array(b.pos, (npos,)).copy() if npos else np.zeros(0, np.uint32)
+        self.read_n_fwd = np.ctypeslib.as_array(b.read_n_fwd, (n,)).copy() if n else np.zeros(0, np.uint32)
         self.work = dict(n_kmer=b.n_kmer, n_occ_blocks=b.n_occ_blocks, n_lf=b.n_lf, n_sa=b.n_sa,
                          n_steps=b.n_steps)
         self._ptr = ptr

@@ -1,0 +1,98 @@
+"""Pins the oracle to the reference's own code.
+
+oracle/ref_emul/build_ref.py compiles the reference's kernel bodies
+(seed_gen.cu) for the CPU, with a warp emulator for the shuffles and the
+batch loop of main() around them.  These tests run that build and the oracle
+on the same index files and reads and compare the text records read by read.
+They need the reference tree, so they run where the reference is present
+(the library is not built elsewhere and the tests skip).
+
+Known, documented differences that the comparison excludes:
+  * MEM mode, a read with exactly one forward record: the reference's MEM
+    filter never writes that record's interval (seed_gen.cu:1110-1113 skip
+    offset 0 and only copy the last offset when it is > 0), so it prints
+    whatever the uncompacted buffer held (here: zero memory, position
+    4294967295).  The oracle uses the record's own interval.
+"""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import pyoracle
+from helpers import build_index, pack, random_reference, sample_reads
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLD = os.path.join(ROOT, "tests", "golden")
+
+
+def _need_ref():
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "ref_emul"))
+    import pyref as pr
+    if not pr.available("zero"):
+        pytest.skip("reference CPU build not present (built from the reference tree by build())")
+    return pr
+
+
+HDR = re.compile(r"^/\*=+(S?MEM) seeds in read no\. (\d+) ")
+
+
+def per_read(text):
+    reads, cur = [], None
+    for ln in text.split("\n"):
+        if HDR.match(ln):
+            cur = [ln]
+            reads.append(cur)
+        elif cur is not None:
+            cur.append(ln)
+    return ["\n".join(r) for r in reads]
+
+
+def compare(prefix, seqs, offs, lens, k, smem, init="zero"):
+    pr = _need_ref()
+    ref_txt = pr.run(prefix, seqs, offs, lens, k, smem, init)
+    oidx = pyoracle.Index(prefix)
+    b = oidx.seed(seqs, offs, lens, k=k, smem=smem)
+    tmp = prefix + ".oracle.txt"
+    b.write_text(tmp, 1, smem)
+    ora = per_read(open(tmp).read())
+    ref = per_read(ref_txt)
+    assert len(ora) == len(ref) == lens.size
+    diff, excluded = [], 0
+    for r in range(lens.size):
+        if not smem and b.read_n_fwd[r] == 1:
+            excluded += 1
+            continue
+        if ora[r] != ref[r]:
+            diff.append(r)
+    return diff, excluded, ora, ref
+
+
+def test_golden_set_matches_reference(built, tmp_path):
+    text = open(os.path.join(GOLD, "ref20k.txt")).read().strip()
+    codes = np.array(["ACGT".index(ch) for ch in text], np.uint8)
+    prefix = build_index(tmp_path, codes, sa_intv=7)
+    reads = [ln.strip().encode() for ln in open(os.path.join(GOLD, "reads60.fa")) if not ln.startswith(">")]
+    seqs, offs, lens = pack(reads)
+    for smem in (True, False):
+        diff, excluded, ora, ref = compare(prefix, seqs, offs, lens, 19, smem)
+        assert not diff, (smem, diff[:5], ora[diff[0]] if diff else "", ref[diff[0]] if diff else "")
+
+
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_random_sets_match_reference(built, tmp_path, case):
+    n = (30_000, 80_000, 50_000)[case]
+    codes = random_reference(n, 300 + case, dups=20)
+    prefix = build_index(tmp_path, codes, sa_intv=(7, 5, 3)[case])
+    ks = ((13, 19), (19, 25), (20, 31))[case]
+    # reads shorter than k - 1 make the reference write outside its slot map
+    # (seed_gen.cu:2630-2632), so every read here is at least max(k) long
+    reads = sample_reads(codes, 150, seed=case, lengths=(31, 40, 60, 100, 150, 250),
+                         err=0.02, n_rate=0.3)
+    seqs, offs, lens = pack(reads)
+    for k in ks:
+        for smem in (True, False):
+            diff, excluded, ora, ref = compare(prefix, seqs, offs, lens, k, smem)
+            assert not diff, (k, smem, diff[:5], ora[diff[0]] if diff else "", ref[diff[0]] if diff else "")
