@@ -29,7 +29,7 @@ EXPORTS = ["gs_index_load", "gs_index_from_host", "gs_index_build", "gs_index_fr
            "gs_index_kmer_table", "gs_index_set_l2_window", "gs_ctx_create", "gs_ctx_free",
            "gs_seed", "gs_seed_device", "gs_result_host", "gs_result_device",
            "gs_result_write_text", "gs_ctx_stream", "gs_ctx_last_timing", "gs_ctx_last_work",
-           "gs_last_error",
+           "gs_seed_noalloc", "gs_last_error",
            "gs_strerror", "gs_version"]
 
 
@@ -93,6 +93,8 @@ def lib():
         L.gs_ctx_stream.restype = vp
         L.gs_ctx_last_timing.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         L.gs_ctx_last_work.argtypes = [vp, vp]
+        L.gs_seed_noalloc.argtypes = [vp, vp, vp, vp, u32, C.POINTER(Params), vp, vp, u64, vp, u64,
+                                      vp, vp, C.POINTER(u64), C.POINTER(u64)]
         L.gs_last_error.restype = C.c_char_p
         L.gs_strerror.restype = C.c_char_p
         L.gs_strerror.argtypes = [i32]
@@ -162,6 +164,21 @@ def build_index(codes, sa_intv: int = 7, prefix: str | None = None, device: int 
     idx = Index.__new__(Index)
     idx.h = h
     return idx
+
+
+def seed_noalloc(index: Index, d_seqs: int, d_offsets: int, d_lengths: int, n_reads: int,
+                 d_seeds: int, seed_cap: int, d_pos: int, pos_cap: int, d_read_seed_off: int,
+                 d_read_pos_off: int, stream: int = 0, **kw):
+    """gs_seed_noalloc: the batched pass with no allocation (device pointers in
+    and out); returns (n_seeds, n_pos)."""
+    p = Context.params(**kw)
+    ns, npos = C.c_uint64(), C.c_uint64()
+    check(lib().gs_seed_noalloc(index.h, C.c_void_p(d_seqs), C.c_void_p(d_offsets),
+                                C.c_void_p(d_lengths), n_reads, C.byref(p),
+                                C.c_void_p(stream) if stream else None, C.c_void_p(d_seeds),
+                                seed_cap, C.c_void_p(d_pos), pos_cap, C.c_void_p(d_read_seed_off),
+                                C.c_void_p(d_read_pos_off), C.byref(ns), C.byref(npos)))
+    return int(ns.value), int(npos.value)
 
 
 class Result:

@@ -144,6 +144,33 @@ int gs_ctx_last_timing(gs_ctx *ctx, float *search_ms, float *total_ms);
  * containment-stopped walk, LF steps and SA samples of the locate stage. */
 int gs_ctx_last_work(gs_ctx *ctx, uint64_t out[4]);
 
+/* ---- allocation-free pass ---------------------------------------------
+ * No counterpart in the reference.  For callers that may not allocate device
+ * memory while they run (a process that fixed its HBM budget at start-up, or
+ * one that cannot let cudaMalloc/cudaFree synchronise the device under other
+ * streams' work): the same batched pass as gs_seed_device, with every scratch
+ * buffer inside one static device array of GS_NOALLOC_SCRATCH_BYTES that the
+ * library keeps on each GPU that loads it.  It allocates nothing; the caller
+ * passes device reads and device output buffers (seeds, positions, per-read
+ * offsets of n_reads + 1 entries) and gets the counts in *n_seeds_out and
+ * *n_pos_out.  Limits per call: GS_NOALLOC_MAX_READS reads,
+ * GS_NOALLOC_MAX_SLOTS candidate slots (2 per start position), seeds and
+ * positions as below; larger inputs are rejected with GS_EINVAL, larger
+ * results with GS_EOVERFLOW (counts still reported).  The first call on a
+ * device looks up the array's device address; make it before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race, so
+ * serialise them. */
+#define GS_NOALLOC_SCRATCH_BYTES (64u << 20)
+#define GS_NOALLOC_MAX_READS 65536u
+#define GS_NOALLOC_MAX_SLOTS (1u << 21)
+#define GS_NOALLOC_MAX_SEEDS (1u << 20)
+#define GS_NOALLOC_MAX_POS (1u << 22)
+int gs_seed_noalloc(gs_index *idx, const char *d_seqs, const uint64_t *d_offsets,
+                    const uint32_t *d_lengths, uint32_t n_reads, const gs_params *p,
+                    void *cuda_stream, gs_seed_rec *d_seeds, uint64_t seed_cap, uint32_t *d_pos,
+                    uint64_t pos_cap, uint64_t *d_read_seed_off, uint64_t *d_read_pos_off,
+                    uint64_t *n_seeds_out, uint64_t *n_pos_out);
+
 /* ---- errors ------------------------------------------------------------- */
 const char *gs_last_error(void);
 const char *gs_strerror(int code);

@@ -1,0 +1,68 @@
+"""The allocation-free entry point gs_seed_noalloc, against gs_seed_device.
+
+gs_seed_noalloc exists for callers that may not allocate device memory while
+they run -- a process that reserved its HBM at start-up, or one that cannot
+let cudaMalloc/cudaFree synchronise the device under other streams' work.
+It runs the same batched pass with all scratch in one static device array.
+Here it is called through the C-ABI twice in a row, on two different batches
+(so the second call starts from the first call's leftovers in the shared
+array), and every seed, position and per-read offset must equal what the
+allocating entry point returns for the same batch (integer results: exact).
+
+This file is named to be collected last.
+"""
+import numpy as np
+import pytest
+
+from helpers import build_index, pack, random_reference, sample_reads
+
+pytestmark = pytest.mark.gpu
+
+
+def test_noalloc_matches_allocating_entry_point(built, tmp_path):
+    import torch
+
+    import gpuseed_gb300 as gs
+
+    codes = random_reference(120_000, 31, dups=30)
+    prefix = build_index(tmp_path, codes, sa_intv=7)
+    idx = gs.Index(prefix)
+    ctx = gs.Context(idx)
+    dev = torch.device("cuda", 0)
+    batches = [sample_reads(codes, 700, seed=41, lengths=(50, 100, 150, 250), err=0.02),
+               sample_reads(codes, 400, seed=42, lengths=(19, 40, 90), err=0.01)]
+    for call, (reads, smem) in enumerate(zip(batches, (True, False))):
+        seqs, offs, lens = pack(reads)
+        d_seqs = torch.from_numpy(np.frombuffer(seqs, np.uint8).copy()).to(dev)
+        d_offs = torch.from_numpy(offs.view(np.int64)).to(dev)
+        d_lens = torch.from_numpy(lens.view(np.int32)).to(dev)
+        n = lens.size
+        want = ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), n,
+                               fetch=True, k=19, smem=smem)
+        seed_cap, pos_cap = want.seeds.shape[0] + 8, want.pos.size + 8
+        d_seeds = torch.zeros(seed_cap * 8, dtype=torch.int32, device=dev)
+        d_pos = torch.zeros(pos_cap, dtype=torch.int32, device=dev)
+        d_rso = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+        d_rpo = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+        torch.cuda.synchronize()
+        ns, npos = gs.seed_noalloc(idx, d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), n,
+                                   d_seeds.data_ptr(), seed_cap, d_pos.data_ptr(), pos_cap,
+                                   d_rso.data_ptr(), d_rpo.data_ptr(), k=19, smem=smem)
+        torch.cuda.synchronize()
+        assert (ns, npos) == (want.seeds.shape[0], want.pos.size), f"call {call}"
+        got_seeds = d_seeds.cpu().numpy().view(np.uint32).reshape(-1, 8)[:ns]
+        assert np.array_equal(got_seeds, want.seeds), f"call {call}: seeds differ"
+        assert np.array_equal(d_pos.cpu().numpy().view(np.uint32)[:npos], want.pos), f"call {call}"
+        assert np.array_equal(d_rso.cpu().numpy().view(np.uint64), want.read_seed_off)
+        assert np.array_equal(d_rpo.cpu().numpy().view(np.uint64), want.read_pos_off)
+        assert ns > 100 and npos >= ns
+
+
+def test_noalloc_rejects_oversized_batch(built, tmp_path):
+    import gpuseed_gb300 as gs
+
+    codes = random_reference(5_000, 32)
+    idx = gs.Index(build_index(tmp_path, codes, sa_intv=7))
+    with pytest.raises(gs.GsError) as e:
+        gs.seed_noalloc(idx, 1, 1, 1, 65537, 1, 1, 1, 1, 1, 1, k=19)
+    assert e.value.code == -1 and "at most 65536" in str(e.value)
