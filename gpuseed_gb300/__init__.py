@@ -25,7 +25,7 @@ GS_ERRORS = {-1: "EINVAL", -2: "EIO", -3: "EFORMAT", -4: "ENOMEM", -5: "ECUDA", 
              -7: "EOVERFLOW", -8: "ETIMEOUT", -9: "ESTATE"}
 
 # Every symbol include/gpuseed.h declares.
-EXPORTS = ["gs_index_load", "gs_index_from_host", "gs_index_build", "gs_index_free", "gs_index_get_info",
+EXPORTS = ["gs_index_load", "gs_index_from_host", "gs_index_build", "gs_index_set_kmer_len", "gs_index_free", "gs_index_get_info",
            "gs_index_kmer_table", "gs_index_set_l2_window", "gs_ctx_create", "gs_ctx_free",
            "gs_seed", "gs_seed_device", "gs_result_host", "gs_result_device",
            "gs_result_write_text", "gs_ctx_stream", "gs_ctx_last_timing", "gs_ctx_last_work",
@@ -60,7 +60,7 @@ class ResultView(C.Structure):
 class IndexInfo(C.Structure):
     _fields_ = [("seq_len", C.c_uint32), ("primary", C.c_uint32), ("sa_intv", C.c_uint32),
                 ("n_sa", C.c_uint32), ("L2", C.c_uint32 * 5), ("device", C.c_int32),
-                ("device_bytes", C.c_uint64)]
+                ("device_bytes", C.c_uint64), ("kmer_len", C.c_int32)]
 
 
 _lib = None
@@ -82,6 +82,7 @@ def lib():
         L.gs_index_get_info.argtypes = [vp, C.POINTER(IndexInfo)]
         L.gs_index_kmer_table.argtypes = [vp, u64, u64, vp]
         L.gs_index_set_l2_window.argtypes = [vp, C.c_float]
+        L.gs_index_set_kmer_len.argtypes = [vp, i32]
         L.gs_ctx_create.argtypes = [vp, vp, C.POINTER(vp)]
         L.gs_ctx_free.argtypes = [vp]
         L.gs_seed.argtypes = [vp, vp, vp, vp, u32, C.POINTER(Params)]
@@ -146,6 +147,9 @@ class Index:
         out = np.empty(2 * count, dtype=np.uint32)
         check(lib().gs_index_kmer_table(self.h, first, count, _ptr(out)))
         return out
+
+    def set_kmer_len(self, kmer_len: int):
+        check(lib().gs_index_set_kmer_len(self.h, kmer_len))
 
     def set_l2_window(self, hit_ratio: float):
         check(lib().gs_index_set_l2_window(self.h, hit_ratio))

@@ -21,9 +21,22 @@ struct gs_index {
     uint32_t *d_occ;
     uint32_t *d_sa;
     uint2 *d_kmer;
-    size_t occ_bytes, sa_bytes, kmer_bytes;
+    uint2 *d_kmerx;
+    size_t occ_bytes, sa_bytes, kmer_bytes, kmerx_bytes;
     float l2_hit_ratio;
 };
+
+extern "C" int gs_index_set_kmer_len(gs_index *idx, int kx);
+
+/* Longer start table by reference length: one table entry per distinct
+ * kx-mer the text can hold (4^kx around seq_len) */
+static int auto_kmer_len(uint32_t seq_len)
+{
+    if (seq_len > (1u << 30)) return 16;
+    if (seq_len > (1u << 28)) return 15;
+    if (seq_len > (1u << 26)) return 14;
+    return GS_K0;
+}
 
 extern "C" void gs_index_free(gs_index *idx);
 
@@ -109,6 +122,10 @@ static int upload(uint32_t primary, const uint32_t L2_1to4[4], const uint32_t *b
         gs_index_free(idx);
         return rc;
     }
+    /* the longer table is an accelerator: without room for it, run without */
+    for (int kx = auto_kmer_len(seq_len); kx > GS_K0; kx--)
+        if (gs_index_set_kmer_len(idx, kx) == GS_OK) break;
+    cudaGetLastError();
     *out = idx;
     return GS_OK;
 }
@@ -208,6 +225,7 @@ extern "C" void gs_index_free(gs_index *idx)
     cudaFree(idx->d_occ);
     cudaFree(idx->d_sa);
     cudaFree(idx->d_kmer);
+    cudaFree(idx->d_kmerx);
     free(idx);
 }
 
@@ -220,7 +238,8 @@ extern "C" int gs_index_get_info(const gs_index *idx, gs_index_info *out)
     out->n_sa = idx->dev.n_sa;
     for (int c = 0; c < 5; c++) out->L2[c] = idx->dev.L2[c];
     out->device = idx->device;
-    out->device_bytes = idx->occ_bytes + idx->sa_bytes + idx->kmer_bytes;
+    out->device_bytes = idx->occ_bytes + idx->sa_bytes + idx->kmer_bytes + idx->kmerx_bytes;
+    out->kmer_len = idx->dev.kx ? idx->dev.kx : GS_K0;
     return GS_OK;
 }
 
@@ -243,5 +262,37 @@ extern "C" int gs_index_set_l2_window(gs_index *idx, float hit_ratio)
 {
     if (!idx || hit_ratio < 0.f || hit_ratio > 1.f) return GS_EINVAL;
     idx->l2_hit_ratio = hit_ratio;
+    return GS_OK;
+}
+
+extern "C" int gs_index_set_kmer_len(gs_index *idx, int kx)
+{
+    if (!idx || kx < GS_K0 || kx > 16) {
+        gs_set_error("k-mer start table length %d outside [13, 16]", kx);
+        return GS_EINVAL;
+    }
+    GS_CUDA(cudaSetDevice(idx->device));
+    if (idx->d_kmerx) {
+        cudaFree(idx->d_kmerx);
+        idx->d_kmerx = NULL;
+        idx->kmerx_bytes = 0;
+    }
+    idx->dev.kmerx = NULL;
+    idx->dev.kx = 0;
+    if (kx == GS_K0) return GS_OK;
+    size_t bytes = (size_t)8 << (2 * kx);
+    uint2 *t = NULL;
+    cudaError_t e = cudaMalloc(&t, bytes);
+    if (e != cudaSuccess) return gs_cuda_fail(e, "cudaMalloc(k-mer start table)");
+    int rc = gs_build_kmerx_table(idx->dev, t, kx, 0);
+    if (rc == GS_OK && (e = cudaDeviceSynchronize()) != cudaSuccess) rc = gs_cuda_fail(e, "k-mer table");
+    if (rc) {
+        cudaFree(t);
+        return rc;
+    }
+    idx->d_kmerx = t;
+    idx->kmerx_bytes = bytes;
+    idx->dev.kmerx = t;
+    idx->dev.kx = kx;
     return GS_OK;
 }

@@ -25,6 +25,8 @@ struct GsDevIndex {
     const uint32_t *occ;
     const uint32_t *sa;
     const uint2 *kmer;
+    const uint2 *kmerx;        /* optional (l,u) table of all kx-mers, same bit order */
+    int32_t kx;                /* 14..16, or 0 when there is no longer table */
     uint32_t primary, seq_len, sa_intv, n_sa;
     uint32_t L2[5];
 };
@@ -84,6 +86,7 @@ int gs_cuda_fail(cudaError_t e, const char *what);
 
 /* kernel launchers (defined next to their kernels) */
 int gs_build_kmer_table(const GsDevIndex &idx, uint2 *table, cudaStream_t st);
+int gs_build_kmerx_table(const GsDevIndex &idx, uint2 *table, int kx, cudaStream_t st);
 int gs_launch_search(const GsDevIndex &idx, GsBatch &b, int kernel, int queue_chunk,
                      int ctas_per_sm, uint32_t n_items, cudaStream_t st);
 int gs_launch_prepare(GsBatch &b, cudaStream_t st);

@@ -48,6 +48,96 @@ int gs_build_kmer_table(const GsDevIndex &I, uint2 *table, cudaStream_t st)
     return GS_OK;
 }
 
+/* longer start table: every kx-mer from its 13-mer prefix (same bit order:
+ * base j at bits 2j, processed first) plus kx-13 steps */
+__global__ void gs_kmerx_kernel(GsDevIndex I, uint2 *table, int kx, uint64_t n)
+{
+    for (uint64_t patt = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; patt < n;
+         patt += (uint64_t)gridDim.x * blockDim.x) {
+        uint2 iv = __ldg(&I.kmer[patt & ((1u << (2 * GS_K0)) - 1u)]);
+        uint32_t l = iv.x, u = iv.y;
+        for (int i = GS_K0; i < kx && l <= u; i++) gs_step(I, l, u, (uint32_t)(patt >> (i << 1)) & 3u);
+        table[patt] = make_uint2(l, u);
+    }
+}
+
+int gs_build_kmerx_table(const GsDevIndex &I, uint2 *table, int kx, cudaStream_t st)
+{
+    uint64_t n = 1ull << (2 * kx);
+    gs_kmerx_kernel<<<152 * 64, 256, 0, st>>>(I, table, kx, n);
+    GS_CUDA(cudaGetLastError());
+    return GS_OK;
+}
+
+/* Start of a candidate: the interval of its first KT bases (forward: the
+ * bases anchor, anchor-1, ...; reverse: the complement codes anchor,
+ * anchor+1, ...; the first base at bits 0-1).  Returns false when one of the
+ * first 13 bases is not ACGT (no search, seed_gen.cu:2132-2143).  A non-ACGT
+ * base at positions 13..KT-1 takes the 13-mer start and steps over it like
+ * the main loop does.  pos = far end reached; alive = interval non-empty. */
+template <int NSTOP>
+__device__ __forceinline__ bool gs_start(const GsDevIndex &I, const unsigned char *seq, int anchor,
+                                         int dir, bool fwd, int KT, uint32_t &l, uint32_t &u,
+                                         int &pos, bool &alive, unsigned long long &w_kmer,
+                                         unsigned long long &w_blk)
+{
+    uint32_t pat = 0;
+    int first_bad = KT;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        if (j < KT) {
+            unsigned char ch = seq[anchor + dir * j];
+            uint32_t c = fwd ? gs_fwd_code(ch) : gs_comp_code(ch);
+            if (c > 3u && first_bad == KT) first_bad = j;
+            pat |= (c & 3u) << (j << 1);
+        }
+    }
+    l = 1;
+    u = 0;
+    alive = false;
+    pos = anchor + dir * (GS_K0 - 1);
+    if (first_bad < GS_K0) return false;
+    w_kmer++;
+    if (first_bad == KT) {
+        uint2 iv = KT == GS_K0 ? __ldg(&I.kmer[pat]) : __ldg(&I.kmerx[pat]);
+        l = iv.x;
+        u = iv.y;
+        pos = anchor + dir * (KT - 1);
+        alive = l <= u;
+        return true;
+    }
+    uint2 iv = __ldg(&I.kmer[pat & ((1u << (2 * GS_K0)) - 1u)]);
+    l = iv.x;
+    u = iv.y;
+    alive = l <= u;
+    for (int j = GS_K0; j < KT && alive; j++) {
+        int np = pos + dir;
+        unsigned char ch = seq[np];
+        uint32_t c = fwd ? gs_fwd_code(ch) : gs_comp_code(ch);
+        if (c > 3u) {
+            if (NSTOP) alive = false;
+            else pos = np;
+        } else {
+            uint32_t nl = l, nu = u;
+            w_blk += (unsigned long long)gs_step(I, nl, nu, c);
+            if (nl > nu) {
+                alive = false;
+            } else {
+                l = nl;
+                u = nu;
+                pos = np;
+            }
+        }
+    }
+    return true;
+}
+
+/* start-table length used for minimum seed length k */
+__device__ __forceinline__ int gs_start_len(const GsDevIndex &I, int k)
+{
+    return (I.kx > GS_K0 && k > I.kx) ? I.kx : GS_K0;
+}
+
 /* ------------------------------------------------------------------ */
 /* per-batch preparation: candidate slots and work items per read */
 
@@ -94,25 +184,13 @@ __device__ __forceinline__ void gs_warp_item(const GsDevIndex &I, const GsBatch 
     /* anchor: e = k-1+ci (fwd), s = n-1-ci (rev); the containing neighbour
      * of every lane is lane+1 */
     int anchor = fwd ? (k - 1 + (int)ci) : ((int)n - 1 - (int)ci);
-    uint32_t l = 1, u = 0;
-    bool ok = in_range;
-    uint32_t pat = 0;
-    if (in_range) {
-#pragma unroll
-        for (int j = 0; j < GS_K0; j++) {
-            uint32_t c = fwd ? gs_fwd_code(seq[anchor - j]) : gs_comp_code(seq[anchor + j]);
-            ok = ok && c <= 3u;
-            pat |= (c & 3u) << (j << 1);
-        }
-    }
-    if (ok) {
-        uint2 iv = __ldg(&I.kmer[pat]);
-        l = iv.x;
-        u = iv.y;
-    }
-    bool alive = ok && l <= u;
-    int pos = fwd ? anchor - (GS_K0 - 1) : anchor + (GS_K0 - 1);
     const int dir = fwd ? -1 : 1;
+    uint32_t l = 1, u = 0;
+    int pos = anchor;
+    bool alive = false, ok = false;
+    unsigned long long wk = 0, wb = 0;
+    if (in_range)
+        ok = gs_start<NSTOP>(I, seq, anchor, dir, fwd, gs_start_len(I, k), l, u, pos, alive, wk, wb);
 
     uint32_t hist[GS_HIST];
 #pragma unroll
@@ -195,7 +273,7 @@ __device__ __forceinline__ void gs_warp_item(const GsDevIndex &I, const GsBatch 
 }
 
 template <int NSTOP>
-__global__ void __launch_bounds__(256) gs_search_batched(GsDevIndex I, GsBatch B, uint32_t n_items,
+__global__ void __launch_bounds__(256, 5) gs_search_batched(GsDevIndex I, GsBatch B, uint32_t n_items,
                                                          int queue_chunk)
 {
     const int lane = threadIdx.x & 31;
@@ -236,6 +314,7 @@ __global__ void __launch_bounds__(128) gs_search_plain(GsDevIndex I, GsBatch B)
     GsRec *slots = B.slots + B.slot_off[r];
     const int iL = (int)L;
     unsigned long long w_kmer = 0, w_blk = 0;
+    const int KT = gs_start_len(I, k);
 
     for (int strand = 0; strand < 2; strand++) {
         const bool fwd = strand == 0;
@@ -243,28 +322,17 @@ __global__ void __launch_bounds__(128) gs_search_plain(GsDevIndex I, GsBatch B)
         for (uint32_t ci = 0; ci < n; ci++) {
             /* forward: e from L-1 down; reverse: s from 0 up */
             int anchor = fwd ? iL - 1 - (int)ci : (int)ci;
-            uint32_t pat = 0;
-            bool ok = true;
-            for (int j = 0; j < GS_K0; j++) {
-                uint32_t c = fwd ? gs_fwd_code(seq[anchor - j]) : gs_comp_code(seq[anchor + j]);
-                if (c > 3u) { ok = false; break; }
-                pat |= c << (j << 1);
-            }
+            const int dir = fwd ? -1 : 1;
             uint32_t l = 1, u = 0;
-            if (ok) {
-                uint2 iv = __ldg(&I.kmer[pat]);
-                l = iv.x;
-                u = iv.y;
-                w_kmer++;
-            }
-            int pos = fwd ? anchor - (GS_K0 - 1) : anchor + (GS_K0 - 1);
+            int pos = anchor;
+            bool alive = false;
+            bool ok = gs_start<NSTOP>(I, seq, anchor, dir, fwd, KT, l, u, pos, alive, w_kmer, w_blk);
             bool killed = false;
-            if (ok && l <= u) {
+            if (alive) {
                 uint32_t sz = u - l + 1u;
                 uint32_t h = H[pos];
                 H[pos] = sz;
                 killed = (h == sz);
-                const int dir = fwd ? -1 : 1;
                 while (!killed) {
                     int np = pos + dir;
                     if (np < 0 || np >= iL) break;

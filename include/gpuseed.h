@@ -86,6 +86,7 @@ typedef struct {
     uint32_t L2[5];
     int32_t device;
     uint64_t device_bytes;          /* HBM held by the index */
+    int32_t kmer_len;               /* start-table length in use (13..16) */
 } gs_index_info;
 
 /* ---- index -------------------------------------------------------------
@@ -110,6 +111,13 @@ int gs_index_kmer_table(const gs_index *idx, uint64_t first, uint64_t count, uin
  * index on `device` into *out when out is not NULL. */
 int gs_index_build(const uint8_t *codes, uint64_t n, uint32_t sa_intv, int device,
                    const char *prefix, gs_index **out);
+/* Length of the k-mer start table (13..16).  Loading picks 16 above 2^30
+ * bases, 15 above 2^28, 14 above 2^26, else 13 (8 * 4^len bytes of HBM; a
+ * lower length is taken when the memory is not there).  A candidate starts
+ * from the interval of its first len bases instead of 13 + len-13 steps: the
+ * SA interval of a string does not depend on how it is found, so results do
+ * not change; seeding uses it only when k > len. */
+int gs_index_set_kmer_len(gs_index *idx, int kmer_len);
 /* Keeps the occurrence table in L2 under an access-policy window on every
  * context stream (fraction of the set-aside, 0 disables). */
 int gs_index_set_l2_window(gs_index *idx, float hit_ratio);

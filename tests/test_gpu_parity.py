@@ -173,3 +173,27 @@ def test_work_counters_match_oracle(small):
         assert w["n_occ_blocks"] == ob.work["n_occ_blocks"]
         assert w["n_lf"] == ob.work["n_lf"]
         assert w["n_sa"] == ob.work["n_sa"]
+
+
+@pytest.mark.parametrize("kx", [14, 16])
+def test_longer_start_table(small, kx):
+    """A 14- or 16-mer start table (used when k > its length) gives the same
+    seeds, including reads whose start window holds an N after base 13."""
+    codes = small["codes"]
+    text = "".join("ACGT"[c] for c in codes)
+    reads = sample_reads(codes, 300, seed=60 + kx, lengths=(20, 40, 100, 150), err=0.03, n_rate=0.5)
+    reads += [(text[3000 + i:3000 + i + 14] + "N" + text[3015 + i:3080 + i]).encode() for i in range(6)]
+    seqs, offs, lens = pack(reads)
+    small["gidx"].set_kmer_len(kx)
+    try:
+        assert small["gidx"].info().kmer_len == kx
+        for kernel in (0, 1):
+            for k in (13, kx, kx + 1, 25):
+                for n_mode in (0, 1):
+                    for smem in (False, True):
+                        gres = small["ctx"].seed(seqs, offs, lens, k=k, smem=smem, n_mode=n_mode,
+                                                 kernel=kernel)
+                        ob = small["oidx"].seed(seqs, offs, lens, k=k, smem=smem, n_mode=n_mode)
+                        assert_same(gres, ob, len(reads), f"kx={kx} kernel={kernel} k={k} n={n_mode}")
+    finally:
+        small["gidx"].set_kmer_len(13)
