@@ -129,6 +129,7 @@ struct gs_ctx {
     uint64_t *seed_pos; size_t cap_seed_pos;
     uint32_t *pos; size_t cap_pos;
     uint32_t *pmap; size_t cap_pmap;
+    GsCont *cont; size_t cap_cont;
     uint32_t *queue;
     uint64_t *d_max;
     unsigned long long *d_work;
@@ -208,6 +209,7 @@ extern "C" void gs_ctx_free(gs_ctx *c)
     cudaFree(c->seed_off); cudaFree(c->pos_off);
     cudaFree(c->slots); cudaFree(c->hist); cudaFree(c->seeds); cudaFree(c->seed_pos);
     cudaFree(c->pos); cudaFree(c->pmap); cudaFree(c->queue); cudaFree(c->d_max);
+    cudaFree(c->cont);
     cudaFree(c->d_work);
     cudaFree(c->cub_tmp);
     cudaFreeHost(c->h_small);
@@ -350,6 +352,12 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     if (p->kernel == GS_KERNEL_PLAIN) {
         RC(grow(c->hist, c->cap_hist, c->h_small[2] + 1));
         B.hist = c->hist;
+    } else if (p->handoff_lanes >= 0) {
+        B.handoff_lanes = p->handoff_lanes ? p->handoff_lanes : GS_HANDOFF_LANES;
+        B.handoff_steps = p->handoff_steps > 0 ? p->handoff_steps : GS_HANDOFF_STEPS;
+        if (B.handoff_lanes > 32) B.handoff_lanes = 32;
+        RC(grow(c->cont, c->cap_cont, (size_t)n_items * (size_t)B.handoff_lanes + 1));
+        B.cont = c->cont;
     }
 
     GS_CUDA(cudaEventRecord(c->ev_s0, st));

@@ -15,6 +15,8 @@
 #define GS_K0 13              /* k-mer table length (seed_gen.cu:2822) */
 #define GS_HIST 8             /* containment history depth of the batched search */
 #define GS_CHUNK 31           /* candidates owned by one warp work item */
+#define GS_HANDOFF_LANES 8    /* default hand-over threshold of the batched search */
+#define GS_HANDOFF_STEPS 4
 
 /* Device view of the index, passed by value to every kernel.
  * occ: one 32-byte block per 64 rows of the $-removed BWT string:
@@ -37,6 +39,14 @@ struct GsRec {
     uint32_t l, u;
 };
 
+/* A candidate handed from the lockstep search to the tail pass. */
+struct GsCont {
+    uint32_t r;
+    int32_t anchor, pos;
+    uint32_t l, u;
+    uint32_t fwd;
+};
+
 /* Per-batch device arguments shared by the pipeline kernels. */
 struct GsBatch {
     const char *seqs;          /* ASCII bases */
@@ -56,8 +66,12 @@ struct GsBatch {
     uint32_t *pos;             /* output positions */
     uint32_t *pmap;            /* position -> seed */
     uint64_t seed_cap, pos_cap;
-    uint32_t *queue;           /* [0]: work-queue head, [1]: status flags */
+    uint32_t *queue;           /* [0]: work-queue head, [1]: status flags,
+                                  [2]: hand-over count, [3]: tail-pass head */
     unsigned long long *work;  /* NULL or [kmer, occ blocks, lf steps, sa samples] */
+    GsCont *cont;              /* NULL: no hand-over; else n_items * handoff_lanes entries */
+    int32_t handoff_lanes;     /* hand over when at most this many owned lanes extend ... */
+    int32_t handoff_steps;     /* ... after at least this many lockstep steps */
 };
 
 #define GS_FLAG_WALK 1u

@@ -165,6 +165,54 @@ int gs_launch_prepare(GsBatch &b, cudaStream_t st)
 /* ------------------------------------------------------------------ */
 /* batched search */
 
+/* one extension step of a candidate; false when it cannot extend further
+ * (read end, empty interval, or a non-ACGT base under GS_N_STOP) */
+template <int NSTOP>
+__device__ __forceinline__ bool gs_advance(const GsDevIndex &I, const unsigned char *seq, int iL,
+                                           bool fwd, int dir, uint32_t &l, uint32_t &u, int &pos)
+{
+    int np = pos + dir;
+    if (np < 0 || np >= iL) return false;
+    uint32_t c = fwd ? gs_fwd_code(seq[np]) : gs_comp_code(seq[np]);
+    if (c > 3u) {
+        if (NSTOP) return false;
+        pos = np;   /* wildcard: interval unchanged */
+        return true;
+    }
+    uint32_t nl = l, nu = u;
+    gs_step(I, nl, nu, c);
+    if (nl > nu) return false;
+    l = nl;
+    u = nu;
+    pos = np;
+    return true;
+}
+
+/* record of a finished candidate (seed_gen.cu:2259-2264, :2398-2404) */
+__device__ __forceinline__ void gs_write_record(const GsBatch &B, uint32_t r, uint32_t n, bool fwd,
+                                                int anchor, int pos, uint32_t l, uint32_t u,
+                                                bool ok, bool killed)
+{
+    const int k = B.k;
+    GsRec rec;
+    rec.x = 0; rec.y = 0; rec.l = l; rec.u = u;
+    if (!killed) {
+        if (fwd) {
+            /* length e - beg with beg = pos-1; a 13-mer that is absent still
+             * counts 13 (the k == 13 case of :2259) */
+            if (ok && anchor - pos + 1 >= k) {
+                rec.x = pos;
+                rec.y = anchor + 1;
+            }
+        } else if (ok && l <= u && pos + 1 - anchor >= k) {
+            rec.x = (int32_t)((uint32_t)anchor | 0x80000000u);
+            rec.y = (int32_t)((uint32_t)(pos + 1) | 0x80000000u);
+        }
+    }
+    uint64_t slot = B.slot_off[r] + (fwd ? (uint64_t)(anchor - (k - 1)) : (uint64_t)n + (uint64_t)anchor);
+    B.slots[slot] = rec;
+}
+
 template <int NSTOP>
 __device__ __forceinline__ void gs_warp_item(const GsDevIndex &I, const GsBatch &B, uint32_t r,
                                              uint32_t local, int lane)
@@ -200,29 +248,9 @@ __device__ __forceinline__ void gs_warp_item(const GsDevIndex &I, const GsBatch 
     int t = 0;
     const uint32_t owned_mask = __ballot_sync(0xffffffffu, owned);
 
+    bool pushed = false;
     while (__ballot_sync(0xffffffffu, alive) & owned_mask) {
-        if (alive) {
-            int np = pos + dir;
-            if (np < 0 || np >= iL) {
-                alive = false;
-            } else {
-                uint32_t c = fwd ? gs_fwd_code(seq[np]) : gs_comp_code(seq[np]);
-                if (c > 3u) {
-                    if (NSTOP) alive = false;
-                    else pos = np;               /* wildcard: interval unchanged */
-                } else {
-                    uint32_t nl = l, nu = u;
-                    gs_step(I, nl, nu, c);
-                    if (nl > nu) {
-                        alive = false;
-                    } else {
-                        l = nl;
-                        u = nu;
-                        pos = np;
-                    }
-                }
-            }
-        }
+        if (alive) alive = gs_advance<NSTOP>(I, seq, iL, fwd, dir, l, u, pos);
         t++;
         uint32_t pub = alive ? u - l + 1u : 0u;
         /* containment: own size d steps ago vs the nearest extending lane
@@ -245,30 +273,79 @@ __device__ __forceinline__ void gs_warp_item(const GsDevIndex &I, const GsBatch 
         for (int m = GS_HIST - 1; m > 0; m--) hist[m] = hist[m - 1];
         hist[0] = cur;
         cur = pub;
+        /* few candidates left: hand them to the tail pass, which walks them
+         * without lockstep, and free the warp */
+        if (B.cont && t >= B.handoff_steps) {
+            uint32_t left = __ballot_sync(0xffffffffu, alive) & owned_mask;
+            if (__popc(left) <= B.handoff_lanes) {
+                bool push = alive && owned;
+                uint32_t base = 0;
+                if (lane == 0 && left) base = atomicAdd(B.queue + 2, (uint32_t)__popc(left));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (push) {
+                    GsCont cst;
+                    cst.r = r;
+                    cst.anchor = anchor;
+                    cst.pos = pos;
+                    cst.l = l;
+                    cst.u = u;
+                    cst.fwd = fwd ? 1u : 0u;
+                    B.cont[base + __popc(left & ((1u << lane) - 1u))] = cst;
+                    pushed = true;
+                }
+                break;
+            }
+        }
     }
 
-    if (owned) {
-        GsRec rec;
-        rec.x = 0; rec.y = 0; rec.l = l; rec.u = u;
-        if (!killed) {
-            if (fwd) {
-                /* length e - beg with beg = pos-1; a 13-mer that is absent
-                 * still counts 13 (the k == 13 case of :2259) */
-                int len = anchor - pos + 1;
-                if (ok && len >= k) {
-                    rec.x = pos;
-                    rec.y = anchor + 1;
-                }
-            } else if (ok && l <= u) {
-                int len = pos + 1 - anchor;
-                if (len >= k) {
-                    rec.x = (int32_t)((uint32_t)anchor | 0x80000000u);
-                    rec.y = (int32_t)((uint32_t)(pos + 1) | 0x80000000u);
+    if (owned && !pushed) gs_write_record(B, r, n, fwd, anchor, pos, l, u, ok, killed);
+}
+
+/* Tail pass: the candidates handed over by gs_search_batched, one per lane;
+ * a lane takes the next one as soon as its own is finished. */
+template <int NSTOP>
+__global__ void __launch_bounds__(256) gs_search_tail(GsDevIndex I, GsBatch B)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t n_cont = *(volatile uint32_t *)(B.queue + 2);
+    bool have = false, exhausted = false;
+    uint32_t r = 0, l = 0, u = 0, n = 0;
+    int anchor = 0, pos = 0, iL = 0, dir = 0;
+    bool fwd = false;
+    const unsigned char *seq = NULL;
+    for (;;) {
+        uint32_t need = __ballot_sync(0xffffffffu, !have && !exhausted);
+        if (need) {
+            int leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(B.queue + 3, (uint32_t)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!have && !exhausted) {
+                uint32_t idx = base + __popc(need & ((1u << lane) - 1u));
+                if (idx < n_cont) {
+                    GsCont c = B.cont[idx];
+                    r = c.r;
+                    anchor = c.anchor;
+                    pos = c.pos;
+                    l = c.l;
+                    u = c.u;
+                    fwd = c.fwd != 0;
+                    dir = fwd ? -1 : 1;
+                    uint32_t L = B.lengths[r];
+                    iL = (int)L;
+                    n = L - (uint32_t)B.k + 1u;
+                    seq = (const unsigned char *)B.seqs + B.offsets[r];
+                    have = true;
+                } else {
+                    exhausted = true;
                 }
             }
         }
-        uint64_t slot = B.slot_off[r] + (fwd ? (uint64_t)(anchor - (k - 1)) : (uint64_t)n + (uint64_t)anchor);
-        B.slots[slot] = rec;
+        if (!__ballot_sync(0xffffffffu, have)) break;
+        if (have && !gs_advance<NSTOP>(I, seq, iL, fwd, dir, l, u, pos)) {
+            gs_write_record(B, r, n, fwd, anchor, pos, l, u, true, false);
+            have = false;
+        }
     }
 }
 
@@ -404,8 +481,15 @@ int gs_launch_search(const GsDevIndex &I, GsBatch &B, int kernel, int queue_chun
     if (need < warps) grid = (need + 7) / 8;
     if (grid == 0) grid = 1;
     GS_CUDA(cudaMemsetAsync(B.queue, 0, sizeof(uint32_t), st));
+    if (B.cont) GS_CUDA(cudaMemsetAsync(B.queue + 2, 0, 2 * sizeof(uint32_t), st));
     if (B.n_mode == GS_N_STOP) gs_search_batched<1><<<grid, 256, 0, st>>>(I, B, n_items, queue_chunk);
     else gs_search_batched<0><<<grid, 256, 0, st>>>(I, B, n_items, queue_chunk);
     GS_CUDA(cudaGetLastError());
+    if (B.cont) {
+        uint32_t tgrid = (uint32_t)sms * 4;
+        if (B.n_mode == GS_N_STOP) gs_search_tail<1><<<tgrid, 256, 0, st>>>(I, B);
+        else gs_search_tail<0><<<tgrid, 256, 0, st>>>(I, B);
+        GS_CUDA(cudaGetLastError());
+    }
     return GS_OK;
 }

@@ -57,6 +57,9 @@ typedef struct {
     int32_t queue_chunk;    /* work items a warp takes per queue grab (0 = auto) */
     int32_t ctas_per_sm;    /* persistent CTAs per SM (0 = auto) */
     int32_t count_work;     /* 1: count algorithmic work (plain kernel walk + locate) */
+    int32_t handoff_lanes;  /* batched: a warp hands its last extending candidates to a
+                               tail pass once at most this many remain (0 = auto, <0 = never) */
+    int32_t handoff_steps;  /* ... but not before this many lockstep steps (0 = auto) */
 } gs_params;
 
 /* One output seed, in output order.  x/y are the reference's int2 read

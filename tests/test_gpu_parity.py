@@ -197,3 +197,18 @@ def test_longer_start_table(small, kx):
                         assert_same(gres, ob, len(reads), f"kx={kx} kernel={kernel} k={k} n={n_mode}")
     finally:
         small["gidx"].set_kmer_len(13)
+
+
+@pytest.mark.parametrize("lanes,steps", [(-1, 0), (1, 1), (8, 4), (32, 1), (32, 30)])
+def test_handoff_settings(small, lanes, steps):
+    """The batched search gives the same seeds whether candidates finish in
+    lockstep or are handed to the tail pass, at any threshold."""
+    reads = sample_reads(small["codes"], 400, seed=70 + lanes, lengths=(30, 100, 150, 300, 700),
+                         err=0.02, n_rate=0.3)
+    seqs, offs, lens = pack(reads)
+    for smem in (False, True):
+        for n_mode in (0, 1):
+            gres = small["ctx"].seed(seqs, offs, lens, k=19, smem=smem, n_mode=n_mode, kernel=0,
+                                     handoff_lanes=lanes, handoff_steps=steps)
+            ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=smem, n_mode=n_mode)
+            assert_same(gres, ob, len(reads), f"handoff {lanes}/{steps} smem={smem} n={n_mode}")
