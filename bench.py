@@ -77,9 +77,8 @@ def workload(cfg, ref_len, n_reads, rank=0, load_gpu_index=True):
     t0 = time.time()
     seqs, offs, lens = W.make_reads(codes, nmask, rspec)
     log(f"[bench] {lens.size:,} reads ({int(lens.sum()):,} bases) in {time.time() - t0:.1f}s")
-    del codes, nmask
     return dict(prefix=prefix, idx=idx, seqs=seqs, offs=offs, lens=lens, k=W.CONFIG_K[cfg],
-                smem=W.CONFIG_SMEM[cfg], spec=spec)
+                smem=W.CONFIG_SMEM[cfg], spec=spec, codes=codes, nmask=nmask)
 
 
 # --------------------------------------------------------------------------
@@ -201,6 +200,59 @@ def cpu_baseline(prefix, seqs, offs, lens, k, smem, table, target_s=12.0, thread
 
 
 # --------------------------------------------------------------------------
+# serving: Poisson arrivals of config-5 requests against the resident index
+
+def serving_sweep(idx, codes, nmask, k, smem, peak_reads_s, loads=(0.1, 0.5, 0.9, 1.2),
+                  seconds=1.5, seed=0x5EED1005):
+    import gpuseed_gb300 as gs
+    from gpuseed_gb300 import workloads as W
+    rng = np.random.default_rng(seed)
+    # request sizes: 1..4096 reads, log-uniform; reads 100-250 bp, 1% errors
+    pool_spec = W.read_spec(5, 400_000)
+    pseqs, poffs, plens = W.make_reads(codes, nmask, pool_spec)
+    mean_reads = (4096 - 1) / np.log(4096)
+    out = []
+    for mode in ("continuous", "per_request"):
+        for load in loads:
+            rate = load * peak_reads_s / mean_reads          # requests per second
+            n_req = max(20, int(rate * seconds))
+            sizes = np.exp(rng.uniform(0, np.log(4096), n_req)).astype(np.int64).clip(1, 4096)
+            gaps = rng.exponential(1.0 / rate, n_req)
+            starts = rng.integers(0, plens.size - 4096, n_req)
+            if mode == "continuous":
+                srv = gs.Server(idx, n_slots=4, k=k, smem=smem)
+            else:
+                srv = gs.Server(idx, n_slots=1, max_batch_reads=1, k=k, smem=smem)
+            ids = []
+            t0 = time.perf_counter()
+            due = t0
+            for i in range(n_req):
+                due += gaps[i]
+                while time.perf_counter() < due:
+                    pass
+                lo, hi = int(starts[i]), int(starts[i] + sizes[i])
+                o = poffs[lo:hi] - poffs[lo]
+                ids.append(srv.submit(pseqs[int(poffs[lo]):int(poffs[hi - 1] + plens[hi - 1])], o,
+                                      plens[lo:hi]))
+            lat = []
+            for rid in ids:
+                srv.wait(rid, -1)
+                lat.append(srv.result(rid)[1])
+            t1 = time.perf_counter()
+            st = srv.stats()
+            srv.stop()
+            out.append({"mode": mode, "load": load, "requests": n_req,
+                        "offered_reads_s": float(sizes.sum() / gaps.sum()),
+                        "achieved_reads_s": float(sizes.sum() / (t1 - t0)),
+                        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                        "passes": int(st["passes"])})
+            log(f"[bench] serving {mode} load {load:.0%}: p50 {out[-1]['p50_ms']:.1f} ms "
+                f"p99 {out[-1]['p99_ms']:.1f} ms, {out[-1]['achieved_reads_s']:,.0f} reads/s, "
+                f"{st['passes']} passes for {n_req} requests")
+    return out
+
+
+# --------------------------------------------------------------------------
 
 def run_reference_arm(args):
     ws, rank, _ = dist_env()
@@ -274,6 +326,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--ref-step-s", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--retune", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -302,9 +356,31 @@ def main():
     d_lens = torch.from_numpy(lens.view(np.int32)).to(dev)
     torch.cuda.synchronize()
 
+    # autotuned launch knobs of the batched search (cached per GPU and workload)
+    tag = f"{torch.cuda.get_device_name(local)}|cfg{args.config}|{w['spec'].length}|{n_reads}|{k}|{smem}"
+    tune_path = os.path.join(CACHE, "autotune.json")
+    cache = {}
+    try:
+        cache = json.load(open(tune_path))
+    except Exception:
+        pass
+    if tag in cache and not args.retune:
+        knobs = cache[tag]["knobs"]
+    else:
+        t0 = time.time()
+        knobs, tms = ctx.autotune(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), n_reads,
+                                  sample=min(n_reads, 1 << 20), k=k, smem=smem)
+        cache[tag] = {"knobs": knobs, "sample_search_ms": tms}
+        try:
+            json.dump(cache, open(tune_path, "w"), indent=1)
+        except OSError:
+            pass
+        log(f"[bench] autotuned {knobs} ({tms:.1f} ms on the sample) in {time.time() - t0:.1f}s")
+
     def step(kernel, count=False):
+        kn = knobs if kernel == gs.KERNEL_BATCHED else {}
         ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), n_reads,
-                        fetch=False, k=k, smem=smem, kernel=kernel, count_work=count)
+                        fetch=False, k=k, smem=smem, kernel=kernel, count_work=count, **kn)
 
     def timed(kernel, steps, warmup, clocks=None):
         for _ in range(warmup):
@@ -387,7 +463,7 @@ def main():
     hs = h_seqs.numpy().view(np.uint8)
     ho = h_offs.numpy().view(np.uint64)
     hl = h_lens.numpy().view(np.uint32)
-    p = ctx.params(k=k, smem=smem)
+    p = ctx.params(k=k, smem=smem, **knobs)
     import ctypes as C2
     for _ in range(2):
         gs.check(L.gs_seed(ctx.h, C2.c_void_p(hs.ctypes.data), C2.c_void_p(ho.ctypes.data),
@@ -407,6 +483,10 @@ def main():
     h2d = int(seqs.nbytes + offs.nbytes + lens.nbytes)
     d2h = int(res.seeds.nbytes + res.pos.nbytes + res.read_seed_off.nbytes + res.read_pos_off.nbytes)
     log(f"[bench] e2e: {e2e_value:,.0f} reads/s")
+
+    latency = None
+    if rank == 0 and not args.no_serving:
+        latency = serving_sweep(idx, w["codes"], w["nmask"], k, smem, value / ws)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -428,12 +508,14 @@ def main():
             "work": work,
             "e2e": {"value": e2e_value, "unit": "reads/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": 6 * args.steps,
+            "gpu_launches": (6 + (1 if knobs.get("handoff_lanes", 0) >= 0 else 0)) * args.steps,
             "clocks": clocks.summary(),
             "roofline": roofline,
             "cpu_baseline": cpu,
-            "latency": None,
+            "latency": latency,
         }
+        line["config"]["autotuned"] = knobs
+        line["config"]["kmer_start_len"] = idx.info().kmer_len
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

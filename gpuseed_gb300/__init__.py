@@ -29,7 +29,9 @@ EXPORTS = ["gs_index_load", "gs_index_from_host", "gs_index_build", "gs_index_se
            "gs_index_kmer_table", "gs_index_set_l2_window", "gs_ctx_create", "gs_ctx_free",
            "gs_seed", "gs_seed_device", "gs_result_host", "gs_result_device",
            "gs_result_write_text", "gs_ctx_stream", "gs_ctx_last_timing", "gs_ctx_last_work",
-           "gs_seed_noalloc", "gs_last_error",
+           "gs_seed_noalloc", "gs_autotune", "gs_server_start", "gs_server_submit", "gs_server_wait",
+           "gs_server_result", "gs_server_release", "gs_server_get_stats", "gs_server_stop",
+           "gs_last_error",
            "gs_strerror", "gs_version"]
 
 
@@ -56,6 +58,17 @@ class ResultView(C.Structure):
     _fields_ = [("n_reads", C.c_uint32), ("n_seeds", C.c_uint64), ("n_pos", C.c_uint64),
                 ("read_seed_off", C.POINTER(C.c_uint64)), ("read_pos_off", C.POINTER(C.c_uint64)),
                 ("seeds", C.POINTER(SeedRec)), ("pos", C.POINTER(C.c_uint32))]
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("n_slots", C.c_int32), ("max_batch_reads", C.c_int32), ("hbm_budget", C.c_uint64),
+                ("params", Params)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("submitted", "completed", "failed", "passes", "reads",
+                                          "max_batch_reads", "pending", "reserved_bytes",
+                                          "budget_bytes")]
 
 
 class IndexInfo(C.Structure):
@@ -95,6 +108,14 @@ def lib():
         L.gs_ctx_stream.restype = vp
         L.gs_ctx_last_timing.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         L.gs_ctx_last_work.argtypes = [vp, vp]
+        L.gs_autotune.argtypes = [vp, vp, vp, vp, u32, C.POINTER(Params), u32, C.POINTER(C.c_float)]
+        L.gs_server_start.argtypes = [vp, C.POINTER(ServerOpts), C.POINTER(vp)]
+        L.gs_server_submit.argtypes = [vp, vp, vp, vp, u32, C.POINTER(u64)]
+        L.gs_server_wait.argtypes = [vp, u64, i32]
+        L.gs_server_result.argtypes = [vp, u64, C.POINTER(ResultView), C.POINTER(C.c_double)]
+        L.gs_server_release.argtypes = [vp, u64]
+        L.gs_server_get_stats.argtypes = [vp, C.POINTER(ServerStats)]
+        L.gs_server_stop.argtypes = [vp]
         L.gs_seed_noalloc.argtypes = [vp, vp, vp, vp, u32, C.POINTER(Params), vp, vp, u64, vp, u64,
                                       vp, vp, C.POINTER(u64), C.POINTER(u64)]
         L.gs_last_error.restype = C.c_char_p
@@ -255,6 +276,17 @@ class Context:
                                    C.c_void_p(d_lengths), n_reads, C.byref(p), 1 if fetch else 0))
         return self.result() if fetch else None
 
+    def autotune(self, d_seqs: int, d_offsets: int, d_lengths: int, n_reads: int,
+                 sample: int = 1 << 20, **kw):
+        """Fastest launch knobs on a sample of device-resident reads: (params dict, search ms)."""
+        p = self.params(**kw)
+        ms = C.c_float()
+        check(lib().gs_autotune(self.h, C.c_void_p(d_seqs), C.c_void_p(d_offsets),
+                                C.c_void_p(d_lengths), n_reads, C.byref(p), sample, C.byref(ms)))
+        knobs = {n: getattr(p, n) for n in ("queue_chunk", "ctas_per_sm", "handoff_lanes",
+                                            "handoff_steps")}
+        return knobs, ms.value
+
     def result(self) -> Result:
         v = ResultView()
         check(lib().gs_result_host(self.h, C.byref(v)))
@@ -281,3 +313,48 @@ class Context:
         a, b = C.c_float(), C.c_float()
         check(lib().gs_ctx_last_timing(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+
+class Server:
+    """Serving loop: resident index, requests merged into passes as slots free up."""
+
+    def __init__(self, index: Index, n_slots=4, max_batch_reads=0, hbm_budget=0, **params):
+        self.index = index
+        o = ServerOpts(n_slots, max_batch_reads, hbm_budget, Context.params(**params))
+        h = C.c_void_p()
+        check(lib().gs_server_start(index.h, C.byref(o), C.byref(h)))
+        self.h = h
+
+    def submit(self, seqs, offsets, lengths) -> int:
+        buf = np.frombuffer(seqs, dtype=np.uint8) if isinstance(seqs, (bytes, bytearray)) else \
+            np.ascontiguousarray(seqs, dtype=np.uint8)
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+        lengths = np.ascontiguousarray(lengths, dtype=np.uint32)
+        rid = C.c_uint64()
+        check(lib().gs_server_submit(self.h, _ptr(buf), _ptr(offsets), _ptr(lengths), lengths.size,
+                                     C.byref(rid)))
+        return rid.value
+
+    def wait(self, rid: int, timeout_ms: int = -1) -> int:
+        return lib().gs_server_wait(self.h, rid, timeout_ms)
+
+    def result(self, rid: int, release: bool = True):
+        v = ResultView()
+        lat = C.c_double()
+        check(lib().gs_server_result(self.h, rid, C.byref(v), C.byref(lat)))
+        res = Result(v)
+        if release:
+            lib().gs_server_release(self.h, rid)
+        return res, lat.value
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        check(lib().gs_server_get_stats(self.h, C.byref(st)))
+        return {n: getattr(st, n) for n, _ in ServerStats._fields_}
+
+    def stop(self):
+        if getattr(self, "h", None):
+            lib().gs_server_stop(self.h)
+            self.h = None
+
+    __del__ = stop

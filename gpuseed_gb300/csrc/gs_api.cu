@@ -592,3 +592,67 @@ extern "C" int gs_result_write_text(gs_ctx *c, int fd, uint32_t first_read_no, i
     }
     return GS_OK;
 }
+
+/* ------------------------------------------------------------------ */
+/* autotuner: coordinate descent over the batched search's launch knobs,
+ * each setting timed (search kernels only, CUDA events) on the first
+ * `sample` reads; the fastest setting is written back into *p. */
+
+extern "C" int gs_autotune(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets,
+                           const uint32_t *d_lengths, uint32_t n_reads, gs_params *p,
+                           uint32_t sample, float *best_ms)
+{
+    if (!c || !p || (n_reads && (!d_seqs || !d_offsets || !d_lengths))) {
+        gs_set_error("gs_autotune: null argument");
+        return GS_EINVAL;
+    }
+    RC(check_params(p));
+    GS_CUDA(cudaSetDevice(gs_index_device(c->idx)));
+    uint32_t n = sample && sample < n_reads ? sample : n_reads;
+    auto eval = [&](const gs_params &q, float &ms) -> int {
+        float best = 1e30f;
+        for (int rep = 0; rep < 2; rep++) {
+            int rc = run_pipeline(c, d_seqs, d_offsets, d_lengths, n, &q, 0);
+            if (rc) return rc;
+            if (rep > 0 || n < 1000) best = c->t_search < best ? c->t_search : best;
+        }
+        ms = best;
+        return GS_OK;
+    };
+    gs_params best = *p;
+    best.kernel = GS_KERNEL_BATCHED;
+    best.count_work = 0;
+    if (!best.queue_chunk) best.queue_chunk = GS_QUEUE_CHUNK;
+    if (!best.handoff_lanes) best.handoff_lanes = GS_HANDOFF_LANES;
+    if (!best.handoff_steps) best.handoff_steps = GS_HANDOFF_STEPS;
+    float bt = 0;
+    RC(eval(best, bt));
+    static const int qcs[] = {1, 2, 4, 8, 16};
+    static const int lanes[] = {-1, 1, 2, 3, 4, 6, 8};
+    static const int steps[] = {2, 3, 4, 6, 8, 12};
+    static const int ctas[] = {0, 2, 3, 4};
+    for (int round = 0; round < 2; round++) {
+        for (int dim = 0; dim < 4; dim++) {
+            const int *vals = dim == 0 ? qcs : dim == 1 ? lanes : dim == 2 ? steps : ctas;
+            int nv = dim == 0 ? 5 : dim == 1 ? 7 : dim == 2 ? 6 : 4;
+            for (int i = 0; i < nv; i++) {
+                gs_params q = best;
+                int *f = dim == 0 ? &q.queue_chunk : dim == 1 ? &q.handoff_lanes
+                         : dim == 2 ? &q.handoff_steps : &q.ctas_per_sm;
+                if (*f == vals[i]) continue;
+                *f = vals[i];
+                float t = 0;
+                RC(eval(q, t));
+                if (t < bt * 0.99f) {
+                    bt = t;
+                    best = q;
+                }
+            }
+        }
+    }
+    best.kernel = p->kernel;
+    best.count_work = p->count_work;
+    *p = best;
+    if (best_ms) *best_ms = bt;
+    return GS_OK;
+}

@@ -15,8 +15,9 @@
 #define GS_K0 13              /* k-mer table length (seed_gen.cu:2822) */
 #define GS_HIST 8             /* containment history depth of the batched search */
 #define GS_CHUNK 31           /* candidates owned by one warp work item */
-#define GS_HANDOFF_LANES 8    /* default hand-over threshold of the batched search */
+#define GS_HANDOFF_LANES 2    /* default hand-over threshold of the batched search */
 #define GS_HANDOFF_STEPS 4
+#define GS_QUEUE_CHUNK 4      /* default work items per queue grab */
 
 /* Device view of the index, passed by value to every kernel.
  * occ: one 32-byte block per 64 rows of the $-removed BWT string:

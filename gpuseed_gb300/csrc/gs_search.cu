@@ -466,7 +466,7 @@ int gs_launch_search(const GsDevIndex &I, GsBatch &B, int kernel, int queue_chun
     int dev = 0, sms = 0;
     GS_CUDA(cudaGetDevice(&dev));
     GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    if (queue_chunk <= 0) queue_chunk = 2;
+    if (queue_chunk <= 0) queue_chunk = GS_QUEUE_CHUNK;
     if (ctas_per_sm <= 0) {
         int occ = 0;
         if (B.n_mode == GS_N_STOP)

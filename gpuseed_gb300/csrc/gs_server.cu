@@ -1,0 +1,348 @@
+/*
+ * gs_server.cu -- serving loop with continuous batching.
+ *
+ * The reference seeds one file batch after another on the default stream
+ * (seed_gen.cu:2910-3790).  Here requests (read sets of any size) arrive at
+ * any time; the index stays resident; n_slots worker threads each own a
+ * context (stream + workspace).  Whenever a slot is free it takes every
+ * pending request that fits -- in arrival order, up to max_batch_reads reads
+ * and within the HBM budget -- merges them into one pass, runs it, and hands
+ * each request its own seeds back.  Passes of different slots overlap on the
+ * device, so a request that arrives while others run is admitted as soon as
+ * a slot and memory free up, not after a whole queue drains.
+ *
+ * Results do not depend on the company a request keeps: every read's seeds
+ * depend on that read alone (the per-read semantics of gs_post.cu), and a
+ * request's reads come back in its own order.
+ */
+#include "gs_internal.h"
+
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <string.h>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+extern "C" int gs_index_get_info(const gs_index *idx, gs_index_info *out);
+int gs_index_device(const gs_index *idx);
+
+namespace {
+
+double now_ms()
+{
+    return std::chrono::duration<double, std::milli>(
+               std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+struct Req {
+    uint64_t id;
+    std::vector<char> seqs;
+    std::vector<uint64_t> offs;
+    std::vector<uint32_t> lens;
+    uint64_t bases;
+    uint64_t est_bytes;
+    double t_submit, t_start, t_done;
+    int status;
+    bool done;
+    std::vector<uint64_t> seed_off, pos_off;
+    std::vector<gs_seed_rec> seeds;
+    std::vector<uint32_t> pos;
+};
+
+/* device bytes one pass needs per base and per read: slots (2 x 16 B per
+ * start position), plain-free batched search, hand-over records, per-read
+ * counters, outputs (a few seeds and positions per read) */
+inline uint64_t estimate_bytes(uint64_t bases, uint64_t reads)
+{
+    return bases * 40 + reads * 256 + (4u << 20);
+}
+
+}  // namespace
+
+struct gs_server {
+    gs_index *idx;
+    gs_server_opts opts;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Req *> pending;
+    std::unordered_map<uint64_t, Req *> reqs;
+    std::vector<std::thread> workers;
+    bool stopping;
+    uint64_t next_id;
+    uint64_t reserved, budget;
+    gs_server_stats stats;
+    int start_error;
+};
+
+static void fail_request(gs_server *s, Req *r, int code)
+{
+    r->status = code;
+    r->done = true;
+    r->t_done = now_ms();
+    s->stats.failed++;
+}
+
+static void worker_main(gs_server *s, int slot)
+{
+    (void)slot;
+    cudaSetDevice(gs_index_device(s->idx));
+    gs_ctx *ctx = NULL;
+    int rc = gs_ctx_create(s->idx, NULL, &ctx);
+    if (rc) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->start_error = rc;
+        s->cv_done.notify_all();
+        return;
+    }
+    std::vector<char> seqs;
+    std::vector<uint64_t> offs;
+    std::vector<uint32_t> lens;
+    std::vector<Req *> batch;
+    for (;;) {
+        uint64_t est = 0;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            s->cv_work.wait(lk, [&] { return s->stopping || !s->pending.empty(); });
+            if (s->stopping && s->pending.empty()) break;
+            batch.clear();
+            uint64_t reads = 0, bases = 0;
+            while (!s->pending.empty()) {
+                Req *r = s->pending.front();
+                uint64_t nr = reads + r->lens.size(), nb = bases + r->bases;
+                uint64_t e = estimate_bytes(nb, nr);
+                if (!batch.empty() &&
+                    (nr > (uint64_t)s->opts.max_batch_reads || s->reserved + e > s->budget))
+                    break;
+                if (batch.empty() && s->reserved + e > s->budget) {
+                    if (s->reserved == 0) {
+                        /* cannot fit even alone on an idle device */
+                        s->pending.pop_front();
+                        fail_request(s, r, GS_ENOMEM);
+                        s->cv_done.notify_all();
+                        continue;
+                    }
+                    break;   /* wait for memory to free up */
+                }
+                s->pending.pop_front();
+                batch.push_back(r);
+                reads = nr;
+                bases = nb;
+                est = e;
+            }
+            if (batch.empty()) {
+                /* memory is held by other slots: wait for a completion */
+                s->cv_done.wait_for(lk, std::chrono::milliseconds(2));
+                continue;
+            }
+            s->reserved += est;
+        }
+        /* merge the requests into one pass */
+        seqs.clear();
+        offs.clear();
+        lens.clear();
+        double t0 = now_ms();
+        for (Req *r : batch) {
+            r->t_start = t0;
+            uint64_t base = seqs.size();
+            seqs.insert(seqs.end(), r->seqs.begin(), r->seqs.end());
+            for (size_t i = 0; i < r->lens.size(); i++) {
+                offs.push_back(base + r->offs[i]);
+                lens.push_back(r->lens[i]);
+            }
+        }
+        rc = gs_seed(ctx, seqs.data(), offs.data(), lens.data(), (uint32_t)lens.size(),
+                     &s->opts.params);
+        gs_result_view v;
+        if (rc == GS_OK) rc = gs_result_host(ctx, &v);
+        /* split */
+        uint64_t read0 = 0;
+        for (Req *r : batch) {
+            if (rc == GS_OK) {
+                uint64_t n = r->lens.size();
+                uint64_t s0 = v.read_seed_off[read0], s1 = v.read_seed_off[read0 + n];
+                uint64_t p0 = v.read_pos_off[read0], p1 = v.read_pos_off[read0 + n];
+                r->seed_off.resize(n + 1);
+                r->pos_off.resize(n + 1);
+                for (uint64_t i = 0; i <= n; i++) {
+                    r->seed_off[i] = v.read_seed_off[read0 + i] - s0;
+                    r->pos_off[i] = v.read_pos_off[read0 + i] - p0;
+                }
+                r->seeds.assign(v.seeds + s0, v.seeds + s1);
+                r->pos.assign(v.pos + p0, v.pos + p1);
+                read0 += n;
+            }
+        }
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            double t1 = now_ms();
+            for (Req *r : batch) {
+                r->status = rc;
+                r->done = true;
+                r->t_done = t1;
+                std::vector<char>().swap(r->seqs);
+                if (rc == GS_OK) s->stats.completed++;
+                else s->stats.failed++;
+            }
+            s->stats.passes++;
+            s->stats.reads += lens.size();
+            if (lens.size() > s->stats.max_batch_reads) s->stats.max_batch_reads = lens.size();
+            s->reserved -= est;
+        }
+        s->cv_done.notify_all();
+        s->cv_work.notify_all();
+    }
+    gs_ctx_free(ctx);
+}
+
+extern "C" int gs_server_start(gs_index *idx, const gs_server_opts *opts, gs_server **out)
+{
+    if (!idx || !opts || !out) {
+        gs_set_error("gs_server_start: null argument");
+        return GS_EINVAL;
+    }
+    *out = NULL;
+    gs_server *s = new gs_server();
+    s->idx = idx;
+    s->opts = *opts;
+    if (s->opts.n_slots <= 0) s->opts.n_slots = 4;
+    if (s->opts.n_slots > 64) s->opts.n_slots = 64;
+    if (s->opts.max_batch_reads <= 0) s->opts.max_batch_reads = 1 << 20;
+    s->stopping = false;
+    s->next_id = 1;
+    s->reserved = 0;
+    s->start_error = 0;
+    memset(&s->stats, 0, sizeof(s->stats));
+    GS_CUDA(cudaSetDevice(gs_index_device(idx)));
+    size_t free_b = 0, total_b = 0;
+    GS_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    s->budget = opts->hbm_budget ? opts->hbm_budget : (uint64_t)(free_b * 0.6);
+    for (int i = 0; i < s->opts.n_slots; i++) s->workers.emplace_back(worker_main, s, i);
+    *out = s;
+    return GS_OK;
+}
+
+extern "C" int gs_server_submit(gs_server *s, const char *seqs, const uint64_t *offsets,
+                                const uint32_t *lengths, uint32_t n_reads, uint64_t *request_id)
+{
+    if (!s || !request_id || (n_reads && (!seqs || !offsets || !lengths))) {
+        gs_set_error("gs_server_submit: null argument");
+        return GS_EINVAL;
+    }
+    if (s->opts.params.k < GS_K0) {
+        gs_set_error("gs_server_submit: server params have k < 13");
+        return GS_EINVAL;
+    }
+    Req *r = new Req();
+    uint64_t bytes = 0;
+    for (uint32_t i = 0; i < n_reads; i++) bytes += lengths[i];
+    r->seqs.resize(bytes);
+    r->offs.resize(n_reads);
+    r->lens.assign(lengths, lengths + n_reads);
+    uint64_t w = 0;
+    for (uint32_t i = 0; i < n_reads; i++) {
+        memcpy(r->seqs.data() + w, seqs + offsets[i], lengths[i]);
+        r->offs[i] = w;
+        w += lengths[i];
+    }
+    r->bases = bytes;
+    r->est_bytes = estimate_bytes(bytes, n_reads);
+    r->done = false;
+    r->status = 0;
+    r->t_submit = now_ms();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->stopping) {
+            delete r;
+            gs_set_error("server is stopping");
+            return GS_ESTATE;
+        }
+        r->id = s->next_id++;
+        s->reqs[r->id] = r;
+        s->pending.push_back(r);
+        s->stats.submitted++;
+        *request_id = r->id;
+    }
+    s->cv_work.notify_one();
+    return GS_OK;
+}
+
+extern "C" int gs_server_wait(gs_server *s, uint64_t id, int32_t timeout_ms)
+{
+    if (!s) return GS_EINVAL;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) {
+        gs_set_error("unknown request %llu", (unsigned long long)id);
+        return GS_EINVAL;
+    }
+    Req *r = it->second;
+    auto pred = [&] { return r->done || s->start_error; };
+    if (timeout_ms < 0) s->cv_done.wait(lk, pred);
+    else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred)) return GS_ETIMEOUT;
+    if (!r->done) {
+        gs_set_error("server worker failed to start");
+        return s->start_error;
+    }
+    return r->status;
+}
+
+extern "C" int gs_server_result(gs_server *s, uint64_t id, gs_result_view *out, double *latency_ms)
+{
+    if (!s || !out) return GS_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end() || !it->second->done) {
+        gs_set_error("request %llu unknown or not finished", (unsigned long long)id);
+        return GS_ESTATE;
+    }
+    Req *r = it->second;
+    if (r->status) return r->status;
+    out->n_reads = (uint32_t)r->lens.size();
+    out->n_seeds = r->seeds.size();
+    out->n_pos = r->pos.size();
+    out->read_seed_off = r->seed_off.data();
+    out->read_pos_off = r->pos_off.data();
+    out->seeds = r->seeds.data();
+    out->pos = r->pos.data();
+    if (latency_ms) *latency_ms = r->t_done - r->t_submit;
+    return GS_OK;
+}
+
+extern "C" int gs_server_release(gs_server *s, uint64_t id)
+{
+    if (!s) return GS_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end() || !it->second->done) return GS_ESTATE;
+    delete it->second;
+    s->reqs.erase(it);
+    return GS_OK;
+}
+
+extern "C" int gs_server_get_stats(gs_server *s, gs_server_stats *out)
+{
+    if (!s || !out) return GS_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->stats;
+    out->pending = s->pending.size();
+    out->reserved_bytes = s->reserved;
+    out->budget_bytes = s->budget;
+    return GS_OK;
+}
+
+extern "C" void gs_server_stop(gs_server *s)
+{
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stopping = true;
+    }
+    s->cv_work.notify_all();
+    for (auto &t : s->workers) t.join();
+    for (auto &kv : s->reqs) delete kv.second;
+    delete s;
+}

@@ -155,6 +155,48 @@ int gs_ctx_last_timing(gs_ctx *ctx, float *search_ms, float *total_ms);
  * containment-stopped walk, LF steps and SA samples of the locate stage. */
 int gs_ctx_last_work(gs_ctx *ctx, uint64_t out[4]);
 
+/* ---- autotuner ----------------------------------------------------------
+ * Times the batched search on the first `sample` reads (device buffers) over
+ * queue_chunk, handoff_lanes, handoff_steps and ctas_per_sm (coordinate
+ * descent, two rounds) and writes the fastest setting into *p; *best_ms gets
+ * its search time.  Results never depend on these knobs. */
+int gs_autotune(gs_ctx *ctx, const char *d_seqs, const uint64_t *d_offsets,
+                const uint32_t *d_lengths, uint32_t n_reads, gs_params *p, uint32_t sample,
+                float *best_ms);
+
+/* ---- serving (continuous batching) ------------------------------------
+ * The reference seeds one file batch after another (seed_gen.cu:2910-3790).
+ * A server keeps the index resident and accepts read sets at any time;
+ * n_slots worker threads, each with its own stream and workspace, merge every
+ * pending request that fits (arrival order, max_batch_reads, HBM budget) into
+ * one pass, so passes of different slots overlap and new requests join as
+ * soon as a slot and memory free up.  A request's seeds depend only on its
+ * reads: the same alone or merged with others. */
+typedef struct gs_server gs_server;
+typedef struct {
+    int32_t n_slots;            /* concurrent passes (default 4) */
+    int32_t max_batch_reads;    /* reads merged into one pass (default 2^20) */
+    uint64_t hbm_budget;        /* workspace bytes the slots may hold together (0: 60% of free) */
+    gs_params params;           /* k, mode, kernel ... applied to every request */
+} gs_server_opts;
+typedef struct {
+    uint64_t submitted, completed, failed, passes, reads, max_batch_reads;
+    uint64_t pending, reserved_bytes, budget_bytes;
+} gs_server_stats;
+int gs_server_start(gs_index *idx, const gs_server_opts *opts, gs_server **out);
+/* Copies the request's reads; the caller's buffers are free on return. */
+int gs_server_submit(gs_server *srv, const char *seqs, const uint64_t *offsets,
+                     const uint32_t *lengths, uint32_t n_reads, uint64_t *request_id);
+/* 0 when done (or the request's error), GS_ETIMEOUT after timeout_ms (< 0: wait). */
+int gs_server_wait(gs_server *srv, uint64_t request_id, int32_t timeout_ms);
+/* Host view of a finished request's seeds (valid until release) and its
+ * submit-to-done latency. */
+int gs_server_result(gs_server *srv, uint64_t request_id, gs_result_view *out, double *latency_ms);
+int gs_server_release(gs_server *srv, uint64_t request_id);
+int gs_server_get_stats(gs_server *srv, gs_server_stats *out);
+/* Finishes the pending requests, then stops the workers. */
+void gs_server_stop(gs_server *srv);
+
 /* ---- allocation-free pass ---------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device
  * memory while they run (a process that fixed its HBM budget at start-up, or
