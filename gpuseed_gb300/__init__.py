@@ -30,7 +30,7 @@ EXPORTS = ["gs_index_load", "gs_index_from_host", "gs_index_build", "gs_index_se
            "gs_seed", "gs_seed_device", "gs_result_host", "gs_result_device",
            "gs_result_write_text", "gs_ctx_stream", "gs_ctx_last_timing", "gs_ctx_last_work",
            "gs_seed_noalloc", "gs_autotune", "gs_server_start", "gs_server_submit", "gs_server_wait",
-           "gs_server_result", "gs_server_release", "gs_server_get_stats", "gs_server_stop",
+           "gs_server_result", "gs_server_release", "gs_server_get_stats", "gs_server_stop", "gs_server_replay",
            "gs_last_error",
            "gs_strerror", "gs_version"]
 
@@ -116,6 +116,8 @@ def lib():
         L.gs_server_release.argtypes = [vp, u64]
         L.gs_server_get_stats.argtypes = [vp, C.POINTER(ServerStats)]
         L.gs_server_stop.argtypes = [vp]
+        L.gs_server_replay.argtypes = [vp, vp, vp, vp, u32, vp, vp, vp, vp, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double)]
         L.gs_seed_noalloc.argtypes = [vp, vp, vp, vp, u32, C.POINTER(Params), vp, vp, u64, vp, u64,
                                       vp, vp, C.POINTER(u64), C.POINTER(u64)]
         L.gs_last_error.restype = C.c_char_p
@@ -346,6 +348,20 @@ class Server:
         if release:
             lib().gs_server_release(self.h, rid)
         return res, lat.value
+
+    def replay(self, pool_seqs, pool_offsets, pool_lengths, first, count, gap_ms):
+        """Submits requests on a schedule from C and waits for all of them:
+        (latencies ms, wall ms, submission span ms)."""
+        first = np.ascontiguousarray(first, dtype=np.uint32)
+        count = np.ascontiguousarray(count, dtype=np.uint32)
+        gap = np.ascontiguousarray(gap_ms, dtype=np.float64)
+        lat = np.zeros(first.size, dtype=np.float64)
+        wall, sub = C.c_double(), C.c_double()
+        check(lib().gs_server_replay(self.h, _ptr(pool_seqs), _ptr(np.ascontiguousarray(pool_offsets, np.uint64)),
+                                     _ptr(np.ascontiguousarray(pool_lengths, np.uint32)), first.size,
+                                     _ptr(first), _ptr(count), _ptr(gap), _ptr(lat), C.byref(wall),
+                                     C.byref(sub)))
+        return lat, wall.value, sub.value
 
     def stats(self) -> dict:
         st = ServerStats()

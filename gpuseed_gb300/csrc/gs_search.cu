@@ -486,7 +486,12 @@ int gs_launch_search(const GsDevIndex &I, GsBatch &B, int kernel, int queue_chun
     else gs_search_batched<0><<<grid, 256, 0, st>>>(I, B, n_items, queue_chunk);
     GS_CUDA(cudaGetLastError());
     if (B.cont) {
-        uint32_t tgrid = (uint32_t)sms * 4;
+        int tocc = 0;
+        if (B.n_mode == GS_N_STOP)
+            GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tocc, gs_search_tail<1>, 256, 0));
+        else
+            GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tocc, gs_search_tail<0>, 256, 0));
+        uint32_t tgrid = (uint32_t)sms * (uint32_t)(tocc > 0 ? tocc : 4);
         if (B.n_mode == GS_N_STOP) gs_search_tail<1><<<tgrid, 256, 0, st>>>(I, B);
         else gs_search_tail<0><<<tgrid, 256, 0, st>>>(I, B);
         GS_CUDA(cudaGetLastError());

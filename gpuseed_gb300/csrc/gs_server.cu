@@ -98,9 +98,11 @@ static void worker_main(gs_server *s, int slot)
         s->cv_done.notify_all();
         return;
     }
-    std::vector<char> seqs;
-    std::vector<uint64_t> offs;
-    std::vector<uint32_t> lens;
+    /* merged batch in pinned host memory: the H2D copy runs at link speed */
+    char *seqs = NULL;
+    uint64_t *offs = NULL;
+    uint32_t *lens = NULL;
+    size_t cap_b = 0, cap_r = 0;
     std::vector<Req *> batch;
     for (;;) {
         uint64_t est = 0;
@@ -141,21 +143,40 @@ static void worker_main(gs_server *s, int slot)
             s->reserved += est;
         }
         /* merge the requests into one pass */
-        seqs.clear();
-        offs.clear();
-        lens.clear();
-        double t0 = now_ms();
+        uint64_t nb = 0, nr = 0;
         for (Req *r : batch) {
-            r->t_start = t0;
-            uint64_t base = seqs.size();
-            seqs.insert(seqs.end(), r->seqs.begin(), r->seqs.end());
-            for (size_t i = 0; i < r->lens.size(); i++) {
-                offs.push_back(base + r->offs[i]);
-                lens.push_back(r->lens[i]);
+            nb += r->bases;
+            nr += r->lens.size();
+        }
+        rc = GS_OK;
+        if (nb + 1 > cap_b) {
+            cudaFreeHost(seqs);
+            cap_b = nb + nb / 2 + 4096;
+            if (cudaMallocHost(&seqs, cap_b) != cudaSuccess) { seqs = NULL; cap_b = 0; rc = GS_ENOMEM; }
+        }
+        if (nr + 1 > cap_r) {
+            cudaFreeHost(offs);
+            cudaFreeHost(lens);
+            cap_r = nr + nr / 2 + 256;
+            if (cudaMallocHost(&offs, cap_r * 8) != cudaSuccess ||
+                cudaMallocHost(&lens, cap_r * 4) != cudaSuccess) {
+                offs = NULL; lens = NULL; cap_r = 0; rc = GS_ENOMEM;
             }
         }
-        rc = gs_seed(ctx, seqs.data(), offs.data(), lens.data(), (uint32_t)lens.size(),
-                     &s->opts.params);
+        double t0 = now_ms();
+        uint64_t wb = 0, wr = 0;
+        if (rc == GS_OK)
+            for (Req *r : batch) {
+                r->t_start = t0;
+                memcpy(seqs + wb, r->seqs.data(), r->bases);
+                for (size_t i = 0; i < r->lens.size(); i++) {
+                    offs[wr] = wb + r->offs[i];
+                    lens[wr] = r->lens[i];
+                    wr++;
+                }
+                wb += r->bases;
+            }
+        if (rc == GS_OK) rc = gs_seed(ctx, seqs, offs, lens, (uint32_t)nr, &s->opts.params);
         gs_result_view v;
         if (rc == GS_OK) rc = gs_result_host(ctx, &v);
         /* split */
@@ -188,13 +209,16 @@ static void worker_main(gs_server *s, int slot)
                 else s->stats.failed++;
             }
             s->stats.passes++;
-            s->stats.reads += lens.size();
-            if (lens.size() > s->stats.max_batch_reads) s->stats.max_batch_reads = lens.size();
+            s->stats.reads += nr;
+            if (nr > s->stats.max_batch_reads) s->stats.max_batch_reads = nr;
             s->reserved -= est;
         }
         s->cv_done.notify_all();
         s->cv_work.notify_all();
     }
+    cudaFreeHost(seqs);
+    cudaFreeHost(offs);
+    cudaFreeHost(lens);
     gs_ctx_free(ctx);
 }
 
@@ -345,4 +369,46 @@ extern "C" void gs_server_stop(gs_server *s)
     for (auto &t : s->workers) t.join();
     for (auto &kv : s->reqs) delete kv.second;
     delete s;
+}
+
+/* Load generator: submits request i (reads first[i] .. first[i]+count[i]-1 of
+ * the pool) gap_ms[i] after request i-1, from this thread, then waits for
+ * all; latency_ms[i] gets each request's submit-to-done time and *wall_ms the
+ * time from the first submission to the last completion. */
+extern "C" int gs_server_replay(gs_server *s, const char *pool_seqs, const uint64_t *pool_offsets,
+                                const uint32_t *pool_lengths, uint32_t n_req, const uint32_t *first,
+                                const uint32_t *count, const double *gap_ms, double *latency_ms,
+                                double *wall_ms, double *submit_ms)
+{
+    if (!s || !pool_seqs || !pool_offsets || !pool_lengths || !first || !count || !gap_ms ||
+        !latency_ms)
+        return GS_EINVAL;
+    std::vector<uint64_t> ids(n_req);
+    std::vector<uint64_t> offs;
+    double t0 = now_ms(), due = t0;
+    for (uint32_t i = 0; i < n_req; i++) {
+        due += gap_ms[i];
+        double now;
+        while ((now = now_ms()) < due) {
+            if (due - now > 0.2) std::this_thread::sleep_for(std::chrono::microseconds(50));
+        }
+        const uint32_t f = first[i], n = count[i];
+        offs.resize(n);
+        uint64_t base = pool_offsets[f];
+        for (uint32_t j = 0; j < n; j++) offs[j] = pool_offsets[f + j] - base;
+        int rc = gs_server_submit(s, pool_seqs + base, offs.data(), pool_lengths + f, n, &ids[i]);
+        if (rc) return rc;
+    }
+    double t_sub = now_ms();
+    int status = GS_OK;
+    for (uint32_t i = 0; i < n_req; i++) {
+        int rc = gs_server_wait(s, ids[i], -1);
+        gs_result_view v;
+        if (rc == GS_OK) rc = gs_server_result(s, ids[i], &v, &latency_ms[i]);
+        if (rc && !status) status = rc;
+        gs_server_release(s, ids[i]);
+    }
+    if (wall_ms) *wall_ms = now_ms() - t0;
+    if (submit_ms) *submit_ms = t_sub - t0;
+    return status;
 }

@@ -82,3 +82,16 @@ extern "C" int gs_probe_random_gather(int device, uint64_t bytes, uint32_t load_
     *gbps = (double)(per * threads) * load_bytes / (best * 1e-3) / 1e9;
     return GS_OK;
 }
+
+extern "C" int gs_set_l2_fetch_granularity(int device, int bytes)
+{
+    if (bytes != 0 && bytes != 32 && bytes != 64 && bytes != 128) {
+        gs_set_error("L2 fetch granularity must be 32, 64 or 128 bytes");
+        return GS_EINVAL;
+    }
+    GS_CUDA(cudaSetDevice(device));
+    if (bytes) GS_CUDA(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)bytes));
+    size_t v = 0;
+    GS_CUDA(cudaDeviceGetLimit(&v, cudaLimitMaxL2FetchGranularity));
+    return (int)v;
+}

@@ -196,6 +196,14 @@ int gs_server_release(gs_server *srv, uint64_t request_id);
 int gs_server_get_stats(gs_server *srv, gs_server_stats *out);
 /* Finishes the pending requests, then stops the workers. */
 void gs_server_stop(gs_server *srv);
+/* Load generator (no counterpart in the reference): submits request i --
+ * reads first[i] .. first[i]+count[i]-1 of a pool -- gap_ms[i] after request
+ * i-1, waits for all, and reports each submit-to-done latency, the wall time
+ * from first submission to last completion and the submission span. */
+int gs_server_replay(gs_server *srv, const char *pool_seqs, const uint64_t *pool_offsets,
+                     const uint32_t *pool_lengths, uint32_t n_req, const uint32_t *first,
+                     const uint32_t *count, const double *gap_ms, double *latency_ms,
+                     double *wall_ms, double *submit_ms);
 
 /* ---- allocation-free pass ---------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device

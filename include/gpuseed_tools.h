@@ -18,6 +18,12 @@ extern "C" {
 int gs_probe_random_gather(int device, uint64_t bytes, uint32_t load_bytes, uint64_t n_loads,
                            double *gbps);
 
+/* Largest L2 fetch from DRAM per miss for this process's context on `device`
+ * (cudaLimitMaxL2FetchGranularity: 32, 64 or 128; 0 only reads it).  Returns
+ * the value in effect (or a negative GS_E* code).  A context limit: it ends
+ * with the process and changes no GPU setting. */
+int gs_set_l2_fetch_granularity(int device, int bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -89,7 +89,7 @@ def test_random_sets_match_reference(built, tmp_path, case):
     ks = ((13, 19), (19, 25), (20, 31))[case]
     # reads shorter than k - 1 make the reference write outside its slot map
     # (seed_gen.cu:2630-2632), so every read here is at least max(k) long
-    reads = sample_reads(codes, 150, seed=case, lengths=(31, 40, 60, 100, 150, 250),
+    reads = sample_reads(codes, 70, seed=case, lengths=(31, 40, 60, 100, 150, 250),
                          err=0.02, n_rate=0.3)
     seqs, offs, lens = pack(reads)
     for k in ks:
