@@ -145,6 +145,14 @@ struct gs_ctx {
     uint64_t n_seeds, n_pos;
     int have_host, have_dev;
     float t_search, t_total;
+    /* captured pass */
+    cudaGraphExec_t gexec;
+    const char *g_seqs;
+    const uint64_t *g_offs;
+    const uint32_t *g_lens;
+    uint32_t g_n;
+    gs_params g_params;
+    uint32_t g_items;
 };
 
 extern "C" int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out)
@@ -219,6 +227,7 @@ extern "C" void gs_ctx_free(gs_ctx *c)
     if (c->ev_s0) cudaEventDestroy(c->ev_s0);
     if (c->ev_s1) cudaEventDestroy(c->ev_s1);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
     if (c->own_stream && c->st) cudaStreamDestroy(c->st);
     free(c);
 }
@@ -349,6 +358,8 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     uint32_t n_items = (uint32_t)(c->h_small[1] & 0xffffffffu);
     RC(grow(c->slots, c->cap_slots, n_slots + 1));
     B.slots = c->slots;
+    B.slot_cap = c->cap_slots;
+    B.item_cap = n_items;
     if (p->kernel == GS_KERNEL_PLAIN) {
         RC(grow(c->hist, c->cap_hist, c->h_small[2] + 1));
         B.hist = c->hist;
@@ -358,6 +369,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
         if (B.handoff_lanes > 32) B.handoff_lanes = 32;
         RC(grow(c->cont, c->cap_cont, (size_t)n_items * (size_t)B.handoff_lanes + 1));
         B.cont = c->cont;
+        B.cont_cap = c->cap_cont;
     }
 
     GS_CUDA(cudaEventRecord(c->ev_s0, st));
@@ -427,6 +439,159 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     return GS_OK;
 }
 
+/* device -> host copy of the last pass's result (sizes known) */
+static int fetch_result(gs_ctx *c)
+{
+    cudaStream_t st = c->st;
+    size_t nr1 = (size_t)c->n_reads + 1;
+    RC(grow_host(c->h_seed_off, c->cap_h_so, nr1));
+    RC(grow_host(c->h_pos_off, c->cap_h_po, nr1));
+    RC(grow_host(c->h_seeds, c->cap_h_seeds, c->n_seeds + 1));
+    RC(grow_host(c->h_pos, c->cap_h_pos, c->n_pos + 1));
+    GS_CUDA(cudaMemcpyAsync(c->h_seed_off, c->seed_off, nr1 * 8, cudaMemcpyDeviceToHost, st));
+    GS_CUDA(cudaMemcpyAsync(c->h_pos_off, c->pos_off, nr1 * 8, cudaMemcpyDeviceToHost, st));
+    if (c->n_seeds)
+        GS_CUDA(cudaMemcpyAsync(c->h_seeds, c->seeds, c->n_seeds * sizeof(gs_seed_rec),
+                                cudaMemcpyDeviceToHost, st));
+    if (c->n_pos)
+        GS_CUDA(cudaMemcpyAsync(c->h_pos, c->pos, c->n_pos * 4, cudaMemcpyDeviceToHost, st));
+    GS_CUDA(cudaStreamSynchronize(st));
+    c->have_host = 1;
+    return GS_OK;
+}
+
+/* Enqueues a whole pass with no host synchronisation: sizes come from the
+ * device (work items, seed and position totals) and every buffer is bounded
+ * by the capacities the context holds; overflow sets a flag. */
+static int enqueue_pass(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets,
+                        const uint32_t *d_lengths, uint32_t n_reads, const gs_params *p)
+{
+    const GsDevIndex &I = *gs_index_dev(c->idx);
+    cudaStream_t st = c->st;
+    size_t nr1 = (size_t)n_reads + 1;
+    GsBatch B;
+    memset(&B, 0, sizeof(B));
+    B.seqs = d_seqs;
+    B.offsets = d_offsets;
+    B.lengths = d_lengths;
+    B.n_reads = n_reads;
+    B.k = p->k;
+    B.smem = p->smem ? 1 : 0;
+    B.n_mode = p->n_mode;
+    B.lf_mode = p->lf_mode;
+    B.queue = c->queue;
+    GS_CUDA(cudaMemsetAsync(c->queue, 0, 16, st));
+    B.slot_off = c->slot_cnt;
+    B.item_off = c->item_cnt;
+    RC(gs_launch_prepare(B, st));
+    RC(exclusive_scan(c, c->slot_cnt, c->slot_off, nr1));
+    RC(exclusive_scan(c, c->item_cnt, c->item_off, nr1));
+    B.slot_off = c->slot_off;
+    B.item_off = c->item_off;
+    B.slots = c->slots;
+    B.slot_cap = c->cap_slots;
+    B.item_cap = c->g_items;
+    if (p->handoff_lanes >= 0 && c->cont) {
+        B.handoff_lanes = p->handoff_lanes ? p->handoff_lanes : GS_HANDOFF_LANES;
+        B.handoff_steps = p->handoff_steps > 0 ? p->handoff_steps : GS_HANDOFF_STEPS;
+        if (B.handoff_lanes > 32) B.handoff_lanes = 32;
+        B.cont = c->cont;
+        B.cont_cap = c->cap_cont;
+    }
+    RC(gs_launch_search(I, B, GS_KERNEL_BATCHED, p->queue_chunk, p->ctas_per_sm, 0, st));
+    B.rd_nf = c->rd_nf;
+    B.rd_nr = c->rd_nr;
+    B.rd_nseeds = c->rd_nseeds;
+    B.rd_npos = c->rd_npos;
+    GS_CUDA(cudaMemsetAsync(c->rd_nseeds + n_reads, 0, 8, st));
+    GS_CUDA(cudaMemsetAsync(c->rd_npos + n_reads, 0, 8, st));
+    RC(gs_launch_finalize_count(I, B, st));
+    RC(exclusive_scan(c, c->rd_nseeds, c->seed_off, nr1));
+    RC(exclusive_scan(c, c->rd_npos, c->pos_off, nr1));
+    B.seed_off = c->seed_off;
+    B.pos_off = c->pos_off;
+    B.seeds = c->seeds;
+    B.seed_pos = c->seed_pos;
+    B.pos = c->pos;
+    B.pmap = c->pmap;
+    B.seed_cap = c->cap_seeds < c->cap_seed_pos ? c->cap_seeds : c->cap_seed_pos;
+    B.pos_cap = c->cap_pos < c->cap_pmap ? c->cap_pos : c->cap_pmap;
+    RC(gs_launch_finalize_emit(I, B, st));
+    RC(gs_launch_locate(I, B, 0, 0, st));
+    return GS_OK;
+}
+
+static bool same_graph(const gs_ctx *c, const char *s, const uint64_t *o, const uint32_t *l,
+                       uint32_t n, const gs_params *p)
+{
+    return c->gexec && c->g_seqs == s && c->g_offs == o && c->g_lens == l && c->g_n == n &&
+           memcmp(&c->g_params, p, sizeof(gs_params)) == 0;
+}
+
+static int run_graph(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets,
+                     const uint32_t *d_lengths, uint32_t n_reads, const gs_params *p, int fetch)
+{
+    cudaStream_t st = c->st;
+    if (same_graph(c, d_seqs, d_offsets, d_lengths, n_reads, p)) {
+        c->have_host = c->have_dev = 0;
+        GS_CUDA(cudaEventRecord(c->ev0, st));
+        GS_CUDA(cudaGraphLaunch(c->gexec, st));
+        GS_CUDA(cudaEventRecord(c->ev1, st));
+        GS_CUDA(cudaMemcpyAsync(&c->h_small[5], c->queue + 1, 4, cudaMemcpyDeviceToHost, st));
+        GS_CUDA(cudaMemcpyAsync(&c->h_small[3], c->seed_off + n_reads, 8, cudaMemcpyDeviceToHost, st));
+        GS_CUDA(cudaMemcpyAsync(&c->h_small[4], c->pos_off + n_reads, 8, cudaMemcpyDeviceToHost, st));
+        GS_CUDA(cudaStreamSynchronize(st));
+        uint32_t flags = (uint32_t)(c->h_small[5] & 0xffffffffu);
+        uint64_t ns = c->h_small[3], np = c->h_small[4];
+        bool fits = !(flags & GS_FLAG_OVERFLOW) && ns <= c->cap_seeds && ns <= c->cap_seed_pos &&
+                    np <= c->cap_pos && np <= c->cap_pmap;
+        if (fits) {
+            if (flags & GS_FLAG_WALK) {
+                gs_set_error("sampled-SA walk exceeded seq_len+2 steps: index inconsistent");
+                return GS_EWALK;
+            }
+            c->n_reads = n_reads;
+            c->n_seeds = ns;
+            c->n_pos = np;
+            c->have_dev = 1;
+            cudaEventElapsedTime(&c->t_total, c->ev0, c->ev1);
+            c->t_search = c->t_total;
+            if (fetch) RC(fetch_result(c));
+            return GS_OK;
+        }
+        /* outgrew the captured pass: size again below */
+    }
+    if (c->gexec) {
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = NULL;
+    }
+    RC(run_pipeline(c, d_seqs, d_offsets, d_lengths, n_reads, p, fetch));
+    if (!c->slots || !c->seeds || !c->pos || !c->seed_pos || !c->pmap) return GS_OK;
+    /* capture a pass with the capacities this one needed */
+    c->g_items = (uint32_t)(c->h_small[1] & 0xffffffffu);
+    cudaGraph_t g = NULL;
+    GS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_pass(c, d_seqs, d_offsets, d_lengths, n_reads, p);
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return gs_cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&c->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        c->gexec = NULL;
+        return gs_cuda_fail(e, "cudaGraphInstantiate");
+    }
+    c->g_seqs = d_seqs;
+    c->g_offs = d_offsets;
+    c->g_lens = d_lengths;
+    c->g_n = n_reads;
+    c->g_params = *p;
+    return GS_OK;
+}
+
 extern "C" int gs_seed_device(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets,
                               const uint32_t *d_lengths, uint32_t n_reads, const gs_params *p,
                               int fetch_to_host)
@@ -437,6 +602,8 @@ extern "C" int gs_seed_device(gs_ctx *c, const char *d_seqs, const uint64_t *d_o
     }
     RC(check_params(p));
     GS_CUDA(cudaSetDevice(gs_index_device(c->idx)));
+    if (p->graph && p->kernel == GS_KERNEL_BATCHED && !p->count_work && n_reads)
+        return run_graph(c, d_seqs, d_offsets, d_lengths, n_reads, p, fetch_to_host);
     return run_pipeline(c, d_seqs, d_offsets, d_lengths, n_reads, p, fetch_to_host);
 }
 

@@ -66,7 +66,10 @@ struct GsBatch {
     uint64_t *seed_pos;        /* per output seed: index of its first position */
     uint32_t *pos;             /* output positions */
     uint32_t *pmap;            /* position -> seed */
-    uint64_t seed_cap, pos_cap;
+    uint64_t seed_cap, pos_cap;   /* output capacities (entries) */
+    uint64_t slot_cap;             /* candidate slots allocated */
+    uint32_t item_cap;             /* work items the hand-over buffer is sized for */
+    uint64_t cont_cap;             /* hand-over records allocated */
     uint32_t *queue;           /* [0]: work-queue head, [1]: status flags,
                                   [2]: hand-over count, [3]: tail-pass head */
     unsigned long long *work;  /* NULL or [kmer, occ blocks, lf steps, sa samples] */
@@ -102,11 +105,15 @@ int gs_cuda_fail(cudaError_t e, const char *what);
 /* kernel launchers (defined next to their kernels) */
 int gs_build_kmer_table(const GsDevIndex &idx, uint2 *table, cudaStream_t st);
 int gs_build_kmerx_table(const GsDevIndex &idx, uint2 *table, int kx, cudaStream_t st);
+/* n_items: host-known work-item count for grid sizing, or 0 (graph capture):
+ * the kernels read the count from item_off[n_reads] on the device */
 int gs_launch_search(const GsDevIndex &idx, GsBatch &b, int kernel, int queue_chunk,
                      int ctas_per_sm, uint32_t n_items, cudaStream_t st);
 int gs_launch_prepare(GsBatch &b, cudaStream_t st);
 int gs_launch_finalize_count(const GsDevIndex &idx, GsBatch &b, cudaStream_t st);
 int gs_launch_finalize_emit(const GsDevIndex &idx, GsBatch &b, cudaStream_t st);
+/* n_seeds / n_pos: host-known totals, or 0 to size the grids by the
+ * capacities and read the totals on the device (graph capture) */
 int gs_launch_locate(const GsDevIndex &idx, GsBatch &b, uint64_t n_seeds, uint64_t n_pos,
                      cudaStream_t st);
 

@@ -163,6 +163,8 @@ extern "C" int gs_seed_noalloc(gs_index *idx, const char *d_seqs, const uint64_t
     B.slot_off = slot_off;
     B.item_off = item_off;
     B.slots = slots;
+    B.slot_cap = GS_NOALLOC_MAX_SLOTS;
+    B.item_cap = n_items;
     NA_RC(gs_launch_search(I, B, GS_KERNEL_BATCHED, p->queue_chunk, p->ctas_per_sm, n_items, st));
 
     /* filters and counts; offsets go straight to the caller's arrays */

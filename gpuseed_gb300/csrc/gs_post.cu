@@ -180,56 +180,66 @@ __global__ void __launch_bounds__(128) gs_finalize_emit(GsBatch B, uint64_t *see
 }
 
 __global__ void __launch_bounds__(256) gs_expand(const uint64_t *seed_pos, const gs_seed_rec *seeds,
-                                                 uint64_t n_seeds, uint32_t *pmap)
+                                                 const uint64_t *n_seeds_dev, uint64_t seed_cap,
+                                                 uint32_t *pmap, uint64_t pos_cap)
 {
-    uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n_seeds) return;
-    uint64_t p = seed_pos[s];
-    uint32_t n = seeds[s].n_pos;
-    for (uint32_t i = 0; i < n; i++) pmap[p + i] = (uint32_t)s;
+    uint64_t n = *n_seeds_dev;
+    if (n > seed_cap) n = seed_cap;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += stride) {
+        uint64_t p = seed_pos[s];
+        uint32_t cnt = seeds[s].n_pos;
+        for (uint32_t i = 0; i < cnt && p + i < pos_cap; i++) pmap[p + i] = (uint32_t)s;
+    }
 }
 
 __global__ void __launch_bounds__(256) gs_locate(GsDevIndex I, const gs_seed_rec *seeds,
                                                  const uint64_t *seed_pos, const uint32_t *pmap,
-                                                 uint64_t n_pos, uint32_t *out, int lf_mode,
-                                                 uint32_t *flags, unsigned long long *work)
+                                                 const uint64_t *n_pos_dev, uint64_t pos_cap,
+                                                 uint32_t *out, int lf_mode, uint32_t *flags,
+                                                 unsigned long long *work)
 {
-    const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t steps = 0;
-    const bool active = j < n_pos;
-    if (active) {
-        uint32_t s = pmap[j];
-        gs_seed_rec S = seeds[s];
-        uint32_t row = S.l + (uint32_t)(j - seed_pos[s]);
-        if (S.xl <= S.xu && row >= S.xl) row += S.xu - S.xl + 1u;
-        /* locate_seeds_gpu (:668-684): LF until a sampled row; a consistent
-         * index reaches one within seq_len+1 steps */
-        const uint32_t cap = I.seq_len + 2u;
-        bool bad = false;
-        while (row % I.sa_intv) {
-            row = gs_lf(I, row, lf_mode);
-            if (++steps > cap) {
-                bad = true;
-                break;
+    uint64_t n_pos = *n_pos_dev;
+    if (n_pos > pos_cap) n_pos = pos_cap;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    /* base is the same for every lane of a warp, so warps stay whole */
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n_pos; base += stride) {
+        const uint64_t j = base + threadIdx.x;
+        uint32_t steps = 0;
+        const bool active = j < n_pos;
+        if (active) {
+            uint32_t s = pmap[j];
+            gs_seed_rec S = seeds[s];
+            uint32_t row = S.l + (uint32_t)(j - seed_pos[s]);
+            if (S.xl <= S.xu && row >= S.xl) row += S.xu - S.xl + 1u;
+            /* locate_seeds_gpu (:668-684): LF until a sampled row; a
+             * consistent index reaches one within seq_len+1 steps */
+            const uint32_t cap = I.seq_len + 2u;
+            bool bad = false;
+            while (row % I.sa_intv) {
+                row = gs_lf(I, row, lf_mode);
+                if (++steps > cap) {
+                    bad = true;
+                    break;
+                }
+            }
+            if (bad) {
+                atomicOr(flags, GS_FLAG_WALK);
+                out[j] = 0xffffffffu;
+            } else {
+                out[j] = __ldg(&I.sa[row / I.sa_intv]) + steps;
             }
         }
-        if (bad) {
-            atomicOr(flags, GS_FLAG_WALK);
-            out[j] = 0xffffffffu;
-        } else {
-            out[j] = __ldg(&I.sa[row / I.sa_intv]) + steps;
-        }
-    }
-    if (work) {
-        /* every lane of the block reaches here: one atomic per warp */
-        unsigned long long st = steps, np = active ? 1ull : 0ull;
-        for (int off = 16; off; off >>= 1) {
-            st += __shfl_xor_sync(0xffffffffu, st, off);
-            np += __shfl_xor_sync(0xffffffffu, np, off);
-        }
-        if ((threadIdx.x & 31) == 0 && np) {
-            atomicAdd(&work[2], st);
-            atomicAdd(&work[3], np);
+        if (work) {
+            unsigned long long st = steps, np = active ? 1ull : 0ull;
+            for (int off = 16; off; off >>= 1) {
+                st += __shfl_xor_sync(0xffffffffu, st, off);
+                np += __shfl_xor_sync(0xffffffffu, np, off);
+            }
+            if ((threadIdx.x & 31) == 0 && np) {
+                atomicAdd(&work[2], st);
+                atomicAdd(&work[3], np);
+            }
         }
     }
 }
@@ -257,13 +267,23 @@ int gs_launch_finalize_emit(const GsDevIndex &I, GsBatch &B, cudaStream_t st)
 int gs_launch_locate(const GsDevIndex &I, GsBatch &B, uint64_t n_seeds, uint64_t n_pos,
                      cudaStream_t st)
 {
-    if (n_seeds == 0 || n_pos == 0) return GS_OK;
-    gs_expand<<<(unsigned)((n_seeds + 255) / 256), 256, 0, st>>>(B.seed_pos, B.seeds, n_seeds,
-                                                                  B.pmap);
+    if (B.n_reads == 0 || B.seed_cap == 0 || B.pos_cap == 0) return GS_OK;
+    uint64_t ns = n_seeds ? n_seeds : B.seed_cap;
+    uint64_t np = n_pos ? n_pos : B.pos_cap;
+    if (n_seeds == 0 && n_pos == 0) {
+        /* totals known only on the device: persistent grids */
+        ns = ns < 152ull * 256 * 32 ? ns : 152ull * 256 * 32;
+        np = np < 152ull * 256 * 64 ? np : 152ull * 256 * 64;
+    } else if (n_pos == 0 || n_seeds == 0) {
+        return GS_OK;   /* nothing to locate */
+    }
+    gs_expand<<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(B.seed_pos, B.seeds,
+                                                             B.seed_off + B.n_reads, B.seed_cap,
+                                                             B.pmap, B.pos_cap);
     GS_CUDA(cudaGetLastError());
-    gs_locate<<<(unsigned)((n_pos + 255) / 256), 256, 0, st>>>(I, B.seeds, B.seed_pos, B.pmap,
-                                                                n_pos, B.pos, B.lf_mode,
-                                                                B.queue + 1, B.work);
+    gs_locate<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(I, B.seeds, B.seed_pos, B.pmap,
+                                                             B.pos_off + B.n_reads, B.pos_cap,
+                                                             B.pos, B.lf_mode, B.queue + 1, B.work);
     GS_CUDA(cudaGetLastError());
     return GS_OK;
 }

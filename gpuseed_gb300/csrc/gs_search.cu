@@ -210,7 +210,8 @@ __device__ __forceinline__ void gs_write_record(const GsBatch &B, uint32_t r, ui
         }
     }
     uint64_t slot = B.slot_off[r] + (fwd ? (uint64_t)(anchor - (k - 1)) : (uint64_t)n + (uint64_t)anchor);
-    B.slots[slot] = rec;
+    if (slot < B.slot_cap) B.slots[slot] = rec;
+    else atomicOr(B.queue + 1, GS_FLAG_OVERFLOW);
 }
 
 template <int NSTOP>
@@ -282,6 +283,10 @@ __device__ __forceinline__ void gs_warp_item(const GsDevIndex &I, const GsBatch 
                 uint32_t base = 0;
                 if (lane == 0 && left) base = atomicAdd(B.queue + 2, (uint32_t)__popc(left));
                 base = __shfl_sync(0xffffffffu, base, 0);
+                if (push && base + __popc(left & ((1u << lane) - 1u)) >= B.cont_cap) {
+                    atomicOr(B.queue + 1, GS_FLAG_OVERFLOW);
+                    push = false;
+                }
                 if (push) {
                     GsCont cst;
                     cst.r = r;
@@ -307,7 +312,8 @@ template <int NSTOP>
 __global__ void __launch_bounds__(256) gs_search_tail(GsDevIndex I, GsBatch B)
 {
     const int lane = threadIdx.x & 31;
-    const uint32_t n_cont = *(volatile uint32_t *)(B.queue + 2);
+    uint32_t n_cont = *(volatile uint32_t *)(B.queue + 2);
+    if (n_cont > B.cont_cap) n_cont = (uint32_t)B.cont_cap;
     bool have = false, exhausted = false;
     uint32_t r = 0, l = 0, u = 0, n = 0;
     int anchor = 0, pos = 0, iL = 0, dir = 0;
@@ -350,10 +356,16 @@ __global__ void __launch_bounds__(256) gs_search_tail(GsDevIndex I, GsBatch B)
 }
 
 template <int NSTOP>
-__global__ void __launch_bounds__(256, 5) gs_search_batched(GsDevIndex I, GsBatch B, uint32_t n_items,
-                                                         int queue_chunk)
+__global__ void __launch_bounds__(256, 5) gs_search_batched(GsDevIndex I, GsBatch B, int queue_chunk)
 {
     const int lane = threadIdx.x & 31;
+    const uint32_t n_items = B.item_off[B.n_reads];
+    if (n_items > B.item_cap) {
+        /* the hand-over buffer was sized for fewer items (a captured pass
+         * replayed on larger input): report, do nothing */
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(B.queue + 1, GS_FLAG_OVERFLOW);
+        return;
+    }
     for (;;) {
         uint32_t first = 0;
         if (lane == 0) first = atomicAdd(B.queue, (uint32_t)queue_chunk);
@@ -476,14 +488,16 @@ int gs_launch_search(const GsDevIndex &I, GsBatch &B, int kernel, int queue_chun
         ctas_per_sm = occ > 0 ? occ : 1;
     }
     uint32_t grid = (uint32_t)sms * (uint32_t)ctas_per_sm;
-    uint32_t need = (n_items + (uint32_t)queue_chunk - 1) / (uint32_t)queue_chunk;
-    uint32_t warps = grid * 8;
-    if (need < warps) grid = (need + 7) / 8;
+    if (n_items) {
+        uint32_t need = (n_items + (uint32_t)queue_chunk - 1) / (uint32_t)queue_chunk;
+        uint32_t warps = grid * 8;
+        if (need < warps) grid = (need + 7) / 8;
+    }
     if (grid == 0) grid = 1;
     GS_CUDA(cudaMemsetAsync(B.queue, 0, sizeof(uint32_t), st));
     if (B.cont) GS_CUDA(cudaMemsetAsync(B.queue + 2, 0, 2 * sizeof(uint32_t), st));
-    if (B.n_mode == GS_N_STOP) gs_search_batched<1><<<grid, 256, 0, st>>>(I, B, n_items, queue_chunk);
-    else gs_search_batched<0><<<grid, 256, 0, st>>>(I, B, n_items, queue_chunk);
+    if (B.n_mode == GS_N_STOP) gs_search_batched<1><<<grid, 256, 0, st>>>(I, B, queue_chunk);
+    else gs_search_batched<0><<<grid, 256, 0, st>>>(I, B, queue_chunk);
     GS_CUDA(cudaGetLastError());
     if (B.cont) {
         int tocc = 0;

@@ -60,6 +60,10 @@ typedef struct {
     int32_t handoff_lanes;  /* batched: a warp hands its last extending candidates to a
                                tail pass once at most this many remain (0 = auto, <0 = never) */
     int32_t handoff_steps;  /* ... but not before this many lockstep steps (0 = auto) */
+    int32_t graph;          /* gs_seed_device: 1 = capture the pass into a CUDA graph on the
+                               first call and replay it while the inputs (pointers, n_reads,
+                               params) repeat; outputs that outgrow the captured capacities
+                               fall back to a sized pass and a new capture */
 } gs_params;
 
 /* One output seed, in output order.  x/y are the reference's int2 read

@@ -1,0 +1,101 @@
+"""The benchmark configurations at their own reference sizes.
+
+* config 2 (100 Mbp, 150 bp, SMEM k=19) and config 4 (long log-normal reads,
+  MEM k=20): GPU-built index, a read subset against the oracle, exact;
+* config 3 (3.1 Gbp, mixed lengths, SMEM k=19): a read sample against the
+  oracle, and over 200,000 reads the size-independent property that every
+  reported position spells the seed: the forward seed's read substring (or the
+  reverse complement of a reverse seed's) occurs in the reference at that
+  position, non-ACGT read bases skipped as the wildcard rule reads them.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_index(tmp, codes, name):
+    import gpuseed_gb300 as gs
+    prefix = os.path.join(str(tmp), name)
+    idx = gs.build_index(codes, 7, prefix=prefix)
+    return prefix, idx
+
+
+def _compare(gres, ob, n):
+    assert gres.n_reads == ob.n_reads == n
+    for r in range(n):
+        assert gres.read_records(r) == ob.read_records(r), f"read {r}"
+
+
+def test_config2_subset(built, tmp_path):
+    import gpuseed_gb300 as gs
+    from gpuseed_gb300 import workloads as W
+    codes, nmask = W.make_reference(W.ref_spec(2))
+    prefix, idx = _gpu_index(tmp_path, codes, "cfg2")
+    seqs, offs, lens = W.make_reads(codes, nmask, W.read_spec(2, 20_000))
+    ctx = gs.Context(idx)
+    oidx = pyoracle.Index(prefix)
+    ob = oidx.seed(seqs, offs, lens, k=19, smem=True)
+    for kernel in (0, 1):
+        _compare(ctx.seed(seqs, offs, lens, k=19, smem=True, kernel=kernel), ob, lens.size)
+    assert any(b"N" in seqs[int(o):int(o) + int(n)].tobytes() for o, n in zip(offs, lens))
+
+
+def test_config4_long_reads(built, tmp_path):
+    import gpuseed_gb300 as gs
+    from gpuseed_gb300 import workloads as W
+    # config-4 reads over the config-2 composition at 100 Mbp
+    codes, nmask = W.make_reference(W.ref_spec(2))
+    prefix, idx = _gpu_index(tmp_path, codes, "cfg4")
+    seqs, offs, lens = W.make_reads(codes, nmask, W.read_spec(4, 1_500))
+    assert lens.min() >= 500 and lens.max() <= 10_000
+    ctx = gs.Context(idx)
+    oidx = pyoracle.Index(prefix)
+    ob = oidx.seed(seqs, offs, lens, k=20, smem=False)
+    gres = ctx.seed(seqs, offs, lens, k=20, smem=False)
+    _compare(gres, ob, lens.size)
+
+
+COMP = np.array([3, 2, 1, 0], np.uint8)
+
+
+def test_config3_full_size(built, tmp_path):
+    import gpuseed_gb300 as gs
+    from gpuseed_gb300 import workloads as W
+    codes, nmask = W.make_reference(W.ref_spec(3))
+    prefix, idx = _gpu_index(tmp_path, codes, "cfg3")
+    assert idx.info().seq_len == 3_100_000_000
+    seqs, offs, lens = W.make_reads(codes, nmask, W.read_spec(3, 200_000))
+    ctx = gs.Context(idx)
+    res = ctx.seed(seqs, offs, lens, k=19, smem=True)
+    # oracle on a sample (13-mer starts computed on the fly: no 512 MiB CPU table)
+    oidx = pyoracle.Index(prefix)
+    m = 1500
+    ob = oidx.seed(seqs, offs[:m], lens[:m], k=19, smem=True)
+    for r in range(m):
+        assert res.read_records(r) == ob.read_records(r), f"read {r}"
+    # every position spells its seed (bwa's LF: the reference's quirk at row
+    # primary+1 would misplace a walk that passes through that row)
+    res = ctx.seed(seqs, offs, lens, k=19, smem=True, lf_mode=gs.LF_BWA)
+    table = np.full(256, 255, np.uint8)
+    for i, ch in enumerate(b"ACGT"):
+        table[ch] = i
+        table[ch + 32] = i
+    checked = 0
+    for r in range(lens.size):
+        read = table[seqs[int(offs[r]):int(offs[r]) + int(lens[r])]]
+        for x, y, l, u, poss in res.read_records(r):
+            b, e = x & 0x7FFFFFFF, y & 0x7FFFFFFF
+            seg = read[b:e]
+            if y >> 31:
+                seg = COMP[seg[::-1][seg[::-1] != 255]]
+            else:
+                seg = seg[seg != 255]
+            for p in poss[:4]:
+                assert np.array_equal(codes[p:p + seg.size], seg), (r, x, y, p)
+                checked += 1
+    assert checked > 200_000
