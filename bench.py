@@ -224,7 +224,7 @@ def serving_sweep(idx, codes, nmask, k, smem, peak_reads_s, loads=(0.1, 0.5, 0.9
             gaps = rng.exponential(1.0 / rate, n_req)
             starts = rng.integers(0, plens.size - 4096, n_req)
             if mode == "continuous":
-                srv = gs.Server(idx, n_slots=4, k=k, smem=smem)
+                srv = gs.Server(idx, n_slots=4, max_batch_reads=1 << 18, k=k, smem=smem)
             else:
                 srv = gs.Server(idx, n_slots=1, max_batch_reads=1, k=k, smem=smem)
             lat, wall_ms, sub_ms = srv.replay(pseqs, poffs, plens, starts, sizes, gaps * 1e3)

@@ -48,8 +48,18 @@ int gs_build_kmer_table(const GsDevIndex &I, uint2 *table, cudaStream_t st)
     return GS_OK;
 }
 
-/* longer start table: every kx-mer from its 13-mer prefix (same bit order:
- * base j at bits 2j, processed first) plus kx-13 steps */
+/* Longer start table, built in three passes over all kx-mers (base j at
+ * bits 2j, processed first, i.e. the string's last character sits at bits
+ * 0-1):
+ *   1. (l,u) from the 13-mer prefix interval plus kx-13 steps;
+ *   2. the forced right extension of each kx-mer X: the base c with
+ *      count(Xc) == count(X) > 0, if any.  Xc's interval is one step with X's
+ *      first character from the kx-mer table entry of (X without its first
+ *      character)·c;
+ *   3. packing: entry.x = l, entry.y = size << 3 | code, code 0-3 the forced
+ *      base, 4 none, 7 "size does not fit 29 bits: start from the 13-mer".
+ * A candidate whose kx-mer is always followed by its neighbour's next base is
+ * contained in that neighbour (see the file comment) and needs no walk. */
 __global__ void gs_kmerx_kernel(GsDevIndex I, uint2 *table, int kx, uint64_t n)
 {
     for (uint64_t patt = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; patt < n;
@@ -61,11 +71,62 @@ __global__ void gs_kmerx_kernel(GsDevIndex I, uint2 *table, int kx, uint64_t n)
     }
 }
 
+__global__ void gs_kmerx_code_kernel(GsDevIndex I, const uint2 *table, int kx, uint64_t n,
+                                     uint8_t *code)
+{
+    const uint64_t mask = n - 1;
+    for (uint64_t X = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; X < n;
+         X += (uint64_t)gridDim.x * blockDim.x) {
+        uint2 e = table[X];
+        uint8_t out = 4;
+        if (e.x <= e.y) {
+            uint32_t size = e.y - e.x + 1u;
+            uint32_t first = (uint32_t)(X >> (2 * (kx - 1))) & 3u;   /* X's first character */
+            for (uint32_t c = 0; c < 4; c++) {
+                uint2 y = table[((X << 2) | c) & mask];
+                if (y.x > y.y) continue;
+                uint32_t l = y.x, u = y.y;
+                gs_step(I, l, u, first);
+                if (l <= u && u - l + 1u == size) {
+                    out = (uint8_t)c;
+                    break;
+                }
+            }
+        }
+        code[X] = out;
+    }
+}
+
+__global__ void gs_kmerx_pack_kernel(uint2 *table, uint64_t n, const uint8_t *code)
+{
+    for (uint64_t X = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; X < n;
+         X += (uint64_t)gridDim.x * blockDim.x) {
+        uint2 e = table[X];
+        uint32_t size = e.x <= e.y ? e.y - e.x + 1u : 0u;
+        uint32_t c = code[X];
+        if (size >= (1u << 29)) {
+            size = 0;
+            c = 7;
+        }
+        table[X] = make_uint2(e.x, (size << 3) | c);
+    }
+}
+
 int gs_build_kmerx_table(const GsDevIndex &I, uint2 *table, int kx, cudaStream_t st)
 {
     uint64_t n = 1ull << (2 * kx);
     gs_kmerx_kernel<<<152 * 64, 256, 0, st>>>(I, table, kx, n);
     GS_CUDA(cudaGetLastError());
+    uint8_t *code = NULL;
+    GS_CUDA(cudaMallocAsync(&code, n, st));
+    gs_kmerx_code_kernel<<<152 * 64, 256, 0, st>>>(I, table, kx, n, code);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        gs_kmerx_pack_kernel<<<152 * 64, 256, 0, st>>>(table, n, code);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(code, st);
+    if (e != cudaSuccess) return gs_cuda_fail(e, "k-mer start table");
     return GS_OK;
 }
 
@@ -74,12 +135,14 @@ int gs_build_kmerx_table(const GsDevIndex &I, uint2 *table, int kx, cudaStream_t
  * anchor+1, ...; the first base at bits 0-1).  Returns false when one of the
  * first 13 bases is not ACGT (no search, seed_gen.cu:2132-2143).  A non-ACGT
  * base at positions 13..KT-1 takes the 13-mer start and steps over it like
- * the main loop does.  pos = far end reached; alive = interval non-empty. */
+ * the main loop does.  pos = far end reached; alive = interval non-empty;
+ * contained = the start string is always followed by the neighbour's next
+ * base (the candidate needs no walk and produces no record). */
 template <int NSTOP>
 __device__ __forceinline__ bool gs_start(const GsDevIndex &I, const unsigned char *seq, int anchor,
-                                         int dir, bool fwd, int KT, uint32_t &l, uint32_t &u,
-                                         int &pos, bool &alive, unsigned long long &w_kmer,
-                                         unsigned long long &w_blk)
+                                         int dir, bool fwd, int KT, int iL, uint32_t &l,
+                                         uint32_t &u, int &pos, bool &alive, bool &contained,
+                                         unsigned long long &w_kmer, unsigned long long &w_blk)
 {
     uint32_t pat = 0;
     int first_bad = KT;
@@ -95,16 +158,36 @@ __device__ __forceinline__ bool gs_start(const GsDevIndex &I, const unsigned cha
     l = 1;
     u = 0;
     alive = false;
+    contained = false;
     pos = anchor + dir * (GS_K0 - 1);
     if (first_bad < GS_K0) return false;
     w_kmer++;
     if (first_bad == KT) {
-        uint2 iv = KT == GS_K0 ? __ldg(&I.kmer[pat]) : __ldg(&I.kmerx[pat]);
-        l = iv.x;
-        u = iv.y;
-        pos = anchor + dir * (KT - 1);
-        alive = l <= u;
-        return true;
+        if (KT == GS_K0) {
+            uint2 iv = __ldg(&I.kmer[pat]);
+            l = iv.x;
+            u = iv.y;
+            pos = anchor + dir * (KT - 1);
+            alive = l <= u;
+            return true;
+        }
+        uint2 iv = __ldg(&I.kmerx[pat]);
+        uint32_t code = iv.y & 7u, size = iv.y >> 3;
+        if (code != 7u) {
+            l = iv.x;
+            u = size ? iv.x + size - 1u : iv.x - 1u;
+            pos = anchor + dir * (KT - 1);
+            alive = size != 0;
+            /* neighbour toward the longer match: e+1 (forward), s-1 (reverse) */
+            int nb = anchor - dir;
+            if (alive && code < 4u && nb >= 0 && nb < iL) {
+                unsigned char ch = seq[nb];
+                uint32_t c = fwd ? gs_fwd_code(ch) : gs_comp_code(ch);
+                contained = (c == code);
+            }
+            return true;
+        }
+        /* interval too wide to pack: the 13-mer start below */
     }
     uint2 iv = __ldg(&I.kmer[pat & ((1u << (2 * GS_K0)) - 1u)]);
     l = iv.x;
@@ -238,14 +321,21 @@ __device__ __forceinline__ void gs_warp_item(const GsDevIndex &I, const GsBatch 
     int pos = anchor;
     bool alive = false, ok = false;
     unsigned long long wk = 0, wb = 0;
-    if (in_range)
-        ok = gs_start<NSTOP>(I, seq, anchor, dir, fwd, gs_start_len(I, k), l, u, pos, alive, wk, wb);
+    bool killed = false;
+    if (in_range) {
+        bool contained = false;
+        ok = gs_start<NSTOP>(I, seq, anchor, dir, fwd, gs_start_len(I, k), iL, l, u, pos, alive,
+                             contained, wk, wb);
+        if (contained) {
+            alive = false;
+            killed = true;
+        }
+    }
 
     uint32_t hist[GS_HIST];
 #pragma unroll
     for (int m = 0; m < GS_HIST; m++) hist[m] = 0;
     uint32_t cur = alive ? u - l + 1u : 0u;
-    bool killed = false;
     int t = 0;
     const uint32_t owned_mask = __ballot_sync(0xffffffffu, owned);
 
@@ -415,8 +505,16 @@ __global__ void __launch_bounds__(128) gs_search_plain(GsDevIndex I, GsBatch B)
             uint32_t l = 1, u = 0;
             int pos = anchor;
             bool alive = false;
-            bool ok = gs_start<NSTOP>(I, seq, anchor, dir, fwd, KT, l, u, pos, alive, w_kmer, w_blk);
-            bool killed = false;
+            bool contained = false;
+            bool ok = gs_start<NSTOP>(I, seq, anchor, dir, fwd, KT, iL, l, u, pos, alive, contained,
+                                      w_kmer, w_blk);
+            bool killed = contained;
+            if (contained) {
+                /* it reached its start level: the candidates to its left may
+                 * compare with it there */
+                H[pos] = u - l + 1u;
+                alive = false;
+            }
             if (alive) {
                 uint32_t sz = u - l + 1u;
                 uint32_t h = H[pos];
