@@ -40,6 +40,19 @@ METRIC = "reads/sec SMEM (bit-exact) batched vs plain kernel on 1 GB300; p50/p99
 CACHE = os.environ.get("GPUSEED_BENCH_CACHE", "/tmp/gpuseed_bench_cache")
 
 
+def nvtx(name):
+    """push an NVTX range (name) or pop the current one (None); no-op when
+    torch was built without NVTX"""
+    import torch
+    try:
+        if name is None:
+            torch.cuda.nvtx.range_pop()
+        else:
+            torch.cuda.nvtx.range_push(name)
+    except Exception:
+        pass
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -382,14 +395,19 @@ def main():
         search_ms = []
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         cm = clocks if clocks is not None else _Null()
+        # NVTX range around the timed steps, so that a profiler can be limited
+        # to them (ncu --nvtx --nvtx-include timed_batched/)
+        rng = "timed_batched" if kernel == gs.KERNEL_BATCHED else "timed_plain"
         with cm:
             torch.cuda.synchronize()
+            nvtx(rng)
             e0.record(st)
             for _ in range(steps):
                 step(kernel, graph=graph)
                 search_ms.append(ctx.last_timing()[0])
             e1.record(st)
             torch.cuda.synchronize()
+            nvtx(None)
         if dist is not None:
             dist.barrier()
         return e0.elapsed_time(e1), search_ms
@@ -433,8 +451,10 @@ def main():
         peak, peak_src = 6800.0, "fallback"
     traffic = None
     try:
-        tj = json.load(open(os.path.join(ROOT, "profiles", "search_traffic.json")))
-        traffic = float(tj["dram_bytes_per_read"]) * n_reads
+        # "dram_bytes_per_read <float>" line of the committed ncu summary
+        for ln in open(os.path.join(ROOT, "profiles", "search_traffic.txt")):
+            if ln.startswith("dram_bytes_per_read "):
+                traffic = float(ln.split()[1]) * n_reads
     except Exception:
         pass
     # random 32-byte gather roofline on a 16 GB buffer
@@ -447,7 +467,7 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
                 "peak_source": f"{peak_src} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
-                "kernel": "gs_search_batched",
+                "kernel": "gs_search_batched + gs_search_tail (one search pass)",
                 "algorithmic_bytes_per_launch": search_bytes,
                 "random_32B_gather_gbs": g32.value,
                 "frac_of_random_32B": achieved / g32.value if g32.value else None}

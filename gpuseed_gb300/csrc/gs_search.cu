@@ -59,7 +59,8 @@ int gs_build_kmer_table(const GsDevIndex &I, uint2 *table, cudaStream_t st)
  *   3. packing: entry.x = l, entry.y = size << 3 | code, code 0-3 the forced
  *      base, 4 none, 7 "size does not fit 29 bits: start from the 13-mer".
  * A candidate whose kx-mer is always followed by its neighbour's next base is
- * contained in that neighbour (see the file comment) and needs no walk. */
+ * contained in that neighbour (see the file comment) and needs no walk;
+ * gs_search_plain stops such candidates at their start. */
 __global__ void gs_kmerx_kernel(GsDevIndex I, uint2 *table, int kx, uint64_t n)
 {
     for (uint64_t patt = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; patt < n;
@@ -136,9 +137,9 @@ int gs_build_kmerx_table(const GsDevIndex &I, uint2 *table, int kx, cudaStream_t
  * first 13 bases is not ACGT (no search, seed_gen.cu:2132-2143).  A non-ACGT
  * base at positions 13..KT-1 takes the 13-mer start and steps over it like
  * the main loop does.  pos = far end reached; alive = interval non-empty;
- * contained = the start string is always followed by the neighbour's next
- * base (the candidate needs no walk and produces no record). */
-template <int NSTOP>
+ * contained (FORCED only) = the start string is always followed by the
+ * neighbour's next base (the candidate needs no walk and produces no record). */
+template <int NSTOP, bool FORCED>
 __device__ __forceinline__ bool gs_start(const GsDevIndex &I, const unsigned char *seq, int anchor,
                                          int dir, bool fwd, int KT, int iL, uint32_t &l,
                                          uint32_t &u, int &pos, bool &alive, bool &contained,
@@ -180,7 +181,7 @@ __device__ __forceinline__ bool gs_start(const GsDevIndex &I, const unsigned cha
             alive = size != 0;
             /* neighbour toward the longer match: e+1 (forward), s-1 (reverse) */
             int nb = anchor - dir;
-            if (alive && code < 4u && nb >= 0 && nb < iL) {
+            if (FORCED && alive && code < 4u && nb >= 0 && nb < iL) {
                 unsigned char ch = seq[nb];
                 uint32_t c = fwd ? gs_fwd_code(ch) : gs_comp_code(ch);
                 contained = (c == code);
@@ -322,14 +323,17 @@ __device__ __forceinline__ void gs_warp_item(const GsDevIndex &I, const GsBatch 
     bool alive = false, ok = false;
     unsigned long long wk = 0, wb = 0;
     bool killed = false;
+    /* The start table's forced extensions are not used here.  A lockstep warp
+     * lasts as long as its longest owned walk; a forced lane dies at step 1
+     * by the neighbour rule anyway, and its step-1 size is what lane-1 is
+     * compared with at step 1 (and lane 31, which nothing kills, is lane 30's
+     * partner for the whole walk).  Stopping forced lanes at their start
+     * saved 4% of the DRAM reads but, after keeping exactly those two
+     * roles, still cost 2.5% of the time (config 3, 10M reads). */
     if (in_range) {
         bool contained = false;
-        ok = gs_start<NSTOP>(I, seq, anchor, dir, fwd, gs_start_len(I, k), iL, l, u, pos, alive,
-                             contained, wk, wb);
-        if (contained) {
-            alive = false;
-            killed = true;
-        }
+        ok = gs_start<NSTOP, false>(I, seq, anchor, dir, fwd, gs_start_len(I, k), iL, l, u, pos,
+                                    alive, contained, wk, wb);
     }
 
     uint32_t hist[GS_HIST];
@@ -506,7 +510,7 @@ __global__ void __launch_bounds__(128) gs_search_plain(GsDevIndex I, GsBatch B)
             int pos = anchor;
             bool alive = false;
             bool contained = false;
-            bool ok = gs_start<NSTOP>(I, seq, anchor, dir, fwd, KT, iL, l, u, pos, alive, contained,
+            bool ok = gs_start<NSTOP, true>(I, seq, anchor, dir, fwd, KT, iL, l, u, pos, alive, contained,
                                       w_kmer, w_blk);
             bool killed = contained;
             if (contained) {

@@ -12,8 +12,10 @@
  *
  * Extra options, off by default: -n (a non-ACGT base stops the extension),
  * -b (bwa's LF at row primary+1), -P (one-read-per-thread search kernel),
- * -B INT (bases per batch).  Errors print a message and exit with status 1,
- * as the reference does for unreadable index files.
+ * -B INT (bases per batch), -F (record-aware input: FASTA records over several
+ * lines, FASTQ, CR LF line ends, a .gz file read through `gzip -dc`; a last
+ * line without a newline keeps its last base).  Errors print a message and
+ * exit with status 1, as the reference does for unreadable index files.
  */
 #define _GNU_SOURCE
 #include <stdint.h>
@@ -32,6 +34,55 @@ static double now_s(void)
     return tv.tv_sec + tv.tv_usec * 1e-6;
 }
 
+/* -F: one record per call, sequence lines joined, CR stripped.  Returns the
+ * sequence length, or -1 at end of input.  FASTQ records (header '@') are
+ * four lines: header, sequence, '+', qualities. */
+static ssize_t next_record(FILE *fp, char **line, size_t *line_cap, char **seq, size_t *seq_cap,
+                           int *pending_header)
+{
+    size_t len = 0;
+    int fastq = 0, have_header = *pending_header;
+    ssize_t n;
+    *pending_header = 0;
+    for (;;) {
+        n = getline(line, line_cap, fp);
+        if (n < 0) break;
+        while (n > 0 && ((*line)[n - 1] == '\n' || (*line)[n - 1] == '\r')) n--;
+        if (n > 0 && ((*line)[0] == '>' || (*line)[0] == '@')) {
+            if (have_header && len > 0) {
+                *pending_header = 1;
+                break;
+            }
+            if (have_header && !fastq && (*line)[0] == '>') { *pending_header = 1; break; }
+            have_header = 1;
+            fastq = (*line)[0] == '@';
+            if (fastq) {
+                ssize_t m = getline(line, line_cap, fp);
+                if (m < 0) break;
+                while (m > 0 && ((*line)[m - 1] == '\n' || (*line)[m - 1] == '\r')) m--;
+                if (len + (size_t)m + 1 > *seq_cap) {
+                    *seq_cap = 2 * (len + (size_t)m + 1);
+                    *seq = (char *)realloc(*seq, *seq_cap);
+                }
+                memcpy(*seq + len, *line, (size_t)m);
+                len += (size_t)m;
+                if (getline(line, line_cap, fp) < 0 || getline(line, line_cap, fp) < 0) break;
+                return (ssize_t)len;
+            }
+            continue;
+        }
+        if (len + (size_t)n + 1 > *seq_cap) {
+            *seq_cap = 2 * (len + (size_t)n + 1);
+            *seq = (char *)realloc(*seq, *seq_cap);
+        }
+        memcpy(*seq + len, *line, (size_t)n);
+        len += (size_t)n;
+        if (!have_header) return (ssize_t)len;   /* headerless: one line, one read */
+    }
+    if (n < 0 && len == 0 && !have_header) return -1;
+    return (ssize_t)len;
+}
+
 static void die(const char *what, int rc)
 {
     fprintf(stderr, "seed_gen: %s: %s (%s)\n", what, gs_strerror(rc), gs_last_error());
@@ -45,8 +96,8 @@ int main(int argc, char *argv[])
     memset(&p, 0, sizeof(p));
     p.k = 20;
     uint64_t batch_bases = 64u << 20;
-    int print_out = 0, c;
-    while ((c = getopt(argc, argv, "k:sonbPB:")) >= 0) {
+    int print_out = 0, records = 0, c;
+    while ((c = getopt(argc, argv, "k:sonbPB:F")) >= 0) {
         switch (c) {
         case 'k': p.k = atoi(optarg); break;
         case 's': p.smem = 1; break;
@@ -55,6 +106,7 @@ int main(int argc, char *argv[])
         case 'b': p.lf_mode = GS_LF_BWA; break;
         case 'P': p.kernel = GS_KERNEL_PLAIN; break;
         case 'B': batch_bases = strtoull(optarg, NULL, 10); break;
+        case 'F': records = 1; break;
         default: break;
         }
     }
@@ -76,7 +128,18 @@ int main(int argc, char *argv[])
     rc = gs_ctx_create(idx, NULL, &ctx);
     if (rc) die("creating context", rc);
 
-    FILE *fp = fopen(argv[optind + 1], "r");
+    const char *fname = argv[optind + 1];
+    size_t fl = strlen(fname);
+    int piped = records && fl > 3 && strcmp(fname + fl - 3, ".gz") == 0;
+    FILE *fp;
+    if (piped) {
+        char *cmd = (char *)malloc(fl + 32);
+        snprintf(cmd, fl + 32, "gzip -dc -- '%s'", fname);
+        fp = popen(cmd, "r");
+        free(cmd);
+    } else {
+        fp = fopen(fname, "r");
+    }
     if (!fp) {
         fprintf(stderr, "seed_gen: cannot open %s\n", argv[optind + 1]);
         return 1;
@@ -85,8 +148,9 @@ int main(int argc, char *argv[])
     char *bases = (char *)malloc(cap_b);
     uint64_t *offs = (uint64_t *)malloc(cap_r * 8);
     uint32_t *lens = (uint32_t *)malloc(cap_r * 4);
-    char *line = NULL;
-    size_t line_cap = 0;
+    char *line = NULL, *rec = NULL;
+    size_t line_cap = 0, rec_cap = 0;
+    int pending_header = 0;
     uint32_t reads_done = 0;
     double t_gpu = 0, t_load = 0, t_print = 0;
     int all_done = 0;
@@ -95,13 +159,26 @@ int main(int argc, char *argv[])
         uint64_t nb = 0;
         uint32_t nr = 0;
         while (nb < batch_bases) {
-            ssize_t n = getline(&line, &line_cap, fp);
-            if (n < 0) {
-                all_done = 1;
-                break;
+            const char *src;
+            size_t L;
+            if (records) {
+                ssize_t n = next_record(fp, &line, &line_cap, &rec, &rec_cap, &pending_header);
+                if (n < 0) {
+                    all_done = 1;
+                    break;
+                }
+                src = rec;
+                L = (size_t)n;
+            } else {
+                ssize_t n = getline(&line, &line_cap, fp);
+                if (n < 0) {
+                    all_done = 1;
+                    break;
+                }
+                if (line[0] == '>') continue;
+                src = line;
+                L = n > 0 ? (size_t)n - 1 : 0;
             }
-            if (line[0] == '>') continue;
-            size_t L = n > 0 ? (size_t)n - 1 : 0;
             if (nb + L + 1 > cap_b) {
                 while (nb + L + 1 > cap_b) cap_b *= 2;
                 bases = (char *)realloc(bases, cap_b);
@@ -115,7 +192,7 @@ int main(int argc, char *argv[])
                 fprintf(stderr, "seed_gen: out of host memory\n");
                 return 1;
             }
-            memcpy(bases + nb, line, L);
+            memcpy(bases + nb, src, L);
             offs[nr] = nb;
             lens[nr] = (uint32_t)L;
             nb += L;
@@ -140,8 +217,10 @@ int main(int argc, char *argv[])
         }
         reads_done += nr;
     }
-    fclose(fp);
+    if (piped) pclose(fp);
+    else fclose(fp);
     free(line);
+    free(rec);
     free(bases);
     free(offs);
     free(lens);

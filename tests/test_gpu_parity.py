@@ -242,3 +242,26 @@ def test_graph_replay(small):
                                    lens0.size, fetch=True, k=19, smem=True, graph=True)
             ob = small["oidx"].seed(buf, packed[0][1], lens0, k=19, smem=True)
             assert_same(gres, ob, lens0.size, f"graph rep {rep}")
+
+
+def test_cli_record_input(small, tmp_path):
+    """seed_gen -F reads multi-line FASTA, FASTQ, CR LF and gzip input; the
+    records equal the oracle's on the joined sequences."""
+    import gzip
+    gs = _gs()
+    reads = sample_reads(small["codes"], 60, seed=123, lengths=(40, 100, 170))
+    seqs, offs, lens = pack(reads)
+    ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=True)
+    want = tmp_path / "o.txt"
+    ob.write_text(str(want), 1, True)
+    fa = b"".join(b">r%d desc\r\n" % i + b"\r\n".join(r[j:j + 33] for j in range(0, len(r), 33)) + b"\r\n"
+                  for i, r in enumerate(reads))
+    fq = b"".join(b"@r%d\n%s\n+\n%s\n" % (i, r, b"I" * len(r)) for i, r in enumerate(reads))
+    files = {"multi.fa": fa, "reads.fq": fq}
+    for name, data in files.items():
+        (tmp_path / name).write_bytes(data)
+    (tmp_path / "multi.fa.gz").write_bytes(gzip.compress(fa))
+    for name in ("multi.fa", "reads.fq", "multi.fa.gz"):
+        out = subprocess.run([gs.CLI_PATH, "-F", "-k", "19", "-s", "-o", small["prefix"],
+                              str(tmp_path / name)], capture_output=True, check=True).stdout
+        assert out == want.read_bytes(), name
