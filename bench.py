@@ -422,6 +422,17 @@ def main():
         step(gs.KERNEL_BATCHED)
         search_ms.append(ctx.last_timing()[0])
     search_ms = search_ms[1:]
+    walkers, walker_cap = ctx.last_walkers()
+    # the lockstep form of the batched search, same pipeline otherwise
+    lock_ms = []
+    for _ in range(3):
+        ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), n_reads,
+                        fetch=False, k=k, smem=smem, kernel=gs.KERNEL_LOCKSTEP, queue_chunk=16,
+                        handoff_lanes=2, handoff_steps=6)
+        lock_ms.append(ctx.last_timing()[0])
+    lock_ms = lock_ms[1:]
+    log(f"[bench] lockstep search {statistics.mean(lock_ms):.1f} ms; batched walkers {walkers:,} "
+        f"(buffer {walker_cap:,})")
     ms = max_over_ranks(dist, ms, dev)
     total_reads = sum_over_ranks(dist, n_reads * args.steps, dev)
     value = total_reads / (ms / 1e3)
@@ -440,6 +451,11 @@ def main():
     step(gs.KERNEL_PLAIN, count=True)
     torch.cuda.synchronize()
     work = ctx.last_work()
+    # lookups the batched search executes (helper lanes, steps before a kill
+    # is seen, walks in the tail pass), same knobs
+    step(gs.KERNEL_BATCHED, count=True)
+    torch.cuda.synchronize()
+    executed = ctx.last_work()
     search_bytes = 32 * (work["n_kmer"] + work["n_occ_blocks"])
     mean_search_s = statistics.mean(search_ms) / 1e3
     achieved = search_bytes / mean_search_s / 1e9
@@ -467,7 +483,7 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
                 "peak_source": f"{peak_src} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
-                "kernel": "gs_search_batched + gs_search_tail (one search pass)",
+                "kernel": "gs_search_start + gs_search_walk (one search pass)",
                 "algorithmic_bytes_per_launch": search_bytes,
                 "random_32B_gather_gbs": g32.value,
                 "frac_of_random_32B": achieved / g32.value if g32.value else None}
@@ -523,10 +539,17 @@ def main():
             "batched_over_plain": value / plain_value,
             "search_ms": statistics.mean(search_ms),
             "seeds_per_step": n_seeds, "positions_per_step": n_pos,
+            "lockstep": {"search_ms": statistics.mean(lock_ms), "knobs": {"queue_chunk": 16,
+                         "handoff_lanes": 2, "handoff_steps": 6}},
+            "walkers": {"handed_to_walk_pass": walkers, "buffer": walker_cap},
             "work": work,
+            "work_executed_batched": {"n_kmer": executed["n_kmer"],
+                                      "n_occ_blocks": executed["n_occ_blocks"],
+                                      "over_canonical": (executed["n_kmer"] + executed["n_occ_blocks"]) /
+                                      max(1, work["n_kmer"] + work["n_occ_blocks"])},
             "e2e": {"value": e2e_value, "unit": "reads/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": (6 + (1 if knobs.get("handoff_lanes", 0) >= 0 else 0)) * args.steps,
+            "gpu_launches": 7 * args.steps,
             "graph": "each timed step replays one CUDA graph of the whole pass",
             "clocks": clocks.summary(),
             "roofline": roofline,

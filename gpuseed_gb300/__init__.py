@@ -19,7 +19,7 @@ CLI_PATH = os.path.join(_PKG, "seed_gen")
 
 N_WILDCARD, N_STOP = 0, 1
 LF_GPUSEED, LF_BWA = 0, 1
-KERNEL_BATCHED, KERNEL_PLAIN = 0, 1
+KERNEL_BATCHED, KERNEL_PLAIN, KERNEL_LOCKSTEP = 0, 1, 2
 
 GS_ERRORS = {-1: "EINVAL", -2: "EIO", -3: "EFORMAT", -4: "ENOMEM", -5: "ECUDA", -6: "EWALK",
              -7: "EOVERFLOW", -8: "ETIMEOUT", -9: "ESTATE"}
@@ -29,6 +29,7 @@ EXPORTS = ["gs_index_load", "gs_index_from_host", "gs_index_build", "gs_index_se
            "gs_index_kmer_table", "gs_index_set_l2_window", "gs_ctx_create", "gs_ctx_free",
            "gs_seed", "gs_seed_device", "gs_result_host", "gs_result_device",
            "gs_result_write_text", "gs_ctx_stream", "gs_ctx_last_timing", "gs_ctx_last_work",
+           "gs_ctx_last_walkers",
            "gs_seed_noalloc", "gs_autotune", "gs_server_start", "gs_server_submit", "gs_server_wait",
            "gs_server_result", "gs_server_release", "gs_server_get_stats", "gs_server_stop", "gs_server_replay",
            "gs_last_error",
@@ -45,7 +46,8 @@ class Params(C.Structure):
     _fields_ = [("k", C.c_int32), ("smem", C.c_int32), ("n_mode", C.c_int32),
                 ("lf_mode", C.c_int32), ("kernel", C.c_int32), ("queue_chunk", C.c_int32),
                 ("ctas_per_sm", C.c_int32), ("count_work", C.c_int32),
-                ("handoff_lanes", C.c_int32), ("handoff_steps", C.c_int32), ("graph", C.c_int32)]
+                ("handoff_lanes", C.c_int32), ("handoff_steps", C.c_int32), ("graph", C.c_int32),
+                ("walker_slots", C.c_int32)]
 
 
 class SeedRec(C.Structure):
@@ -108,6 +110,7 @@ def lib():
         L.gs_ctx_stream.restype = vp
         L.gs_ctx_last_timing.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         L.gs_ctx_last_work.argtypes = [vp, vp]
+        L.gs_ctx_last_walkers.argtypes = [vp, C.POINTER(u64), C.POINTER(u64)]
         L.gs_autotune.argtypes = [vp, vp, vp, vp, u32, C.POINTER(Params), u32, C.POINTER(C.c_float)]
         L.gs_server_start.argtypes = [vp, C.POINTER(ServerOpts), C.POINTER(vp)]
         L.gs_server_submit.argtypes = [vp, vp, vp, vp, u32, C.POINTER(u64)]
@@ -255,9 +258,10 @@ class Context:
     @staticmethod
     def params(k=20, smem=False, n_mode=N_WILDCARD, lf_mode=LF_GPUSEED, kernel=KERNEL_BATCHED,
                queue_chunk=0, ctas_per_sm=0, count_work=False, handoff_lanes=0,
-               handoff_steps=0, graph=False) -> Params:
+               handoff_steps=0, graph=False, walker_slots=0) -> Params:
         return Params(k, 1 if smem else 0, n_mode, lf_mode, kernel, queue_chunk, ctas_per_sm,
-                      1 if count_work else 0, handoff_lanes, handoff_steps, 1 if graph else 0)
+                      1 if count_work else 0, handoff_lanes, handoff_steps, 1 if graph else 0,
+                      walker_slots)
 
     def seed(self, seqs, offsets, lengths, **kw) -> Result:
         """Reads in host memory; returns the host result."""
@@ -310,6 +314,12 @@ class Context:
         a = np.zeros(4, dtype=np.uint64)
         check(lib().gs_ctx_last_work(self.h, _ptr(a)))
         return dict(n_kmer=int(a[0]), n_occ_blocks=int(a[1]), n_lf=int(a[2]), n_sa=int(a[3]))
+
+    def last_walkers(self):
+        """(walkers handed to the walk pass, buffer capacity) of the last batched pass."""
+        n, cap = C.c_uint64(), C.c_uint64()
+        check(lib().gs_ctx_last_walkers(self.h, C.byref(n), C.byref(cap)))
+        return int(n.value), int(cap.value)
 
     def last_timing(self):
         a, b = C.c_float(), C.c_float()

@@ -130,6 +130,8 @@ struct gs_ctx {
     uint32_t *pos; size_t cap_pos;
     uint32_t *pmap; size_t cap_pmap;
     GsCont *cont; size_t cap_cont;
+    GsWalker *walkers; size_t cap_walkers;
+    uint64_t last_walkers, last_walker_cap;
     uint32_t *queue;
     uint64_t *d_max;
     unsigned long long *d_work;
@@ -218,6 +220,7 @@ extern "C" void gs_ctx_free(gs_ctx *c)
     cudaFree(c->slots); cudaFree(c->hist); cudaFree(c->seeds); cudaFree(c->seed_pos);
     cudaFree(c->pos); cudaFree(c->pmap); cudaFree(c->queue); cudaFree(c->d_max);
     cudaFree(c->cont);
+    cudaFree(c->walkers);
     cudaFree(c->d_work);
     cudaFree(c->cub_tmp);
     cudaFreeHost(c->h_small);
@@ -238,6 +241,14 @@ extern "C" int gs_ctx_last_work(gs_ctx *c, uint64_t out[4])
 {
     if (!c || !out) return GS_EINVAL;
     memcpy(out, c->work, sizeof(c->work));
+    return GS_OK;
+}
+
+extern "C" int gs_ctx_last_walkers(gs_ctx *c, uint64_t *n_walkers, uint64_t *capacity)
+{
+    if (!c) return GS_EINVAL;
+    if (n_walkers) *n_walkers = c->last_walkers;
+    if (capacity) *capacity = c->last_walker_cap;
     return GS_OK;
 }
 
@@ -287,7 +298,8 @@ static int check_params(const gs_params *p)
     }
     if ((p->n_mode != GS_N_WILDCARD && p->n_mode != GS_N_STOP) ||
         (p->lf_mode != GS_LF_GPUSEED && p->lf_mode != GS_LF_BWA) ||
-        (p->kernel != GS_KERNEL_BATCHED && p->kernel != GS_KERNEL_PLAIN)) {
+        (p->kernel != GS_KERNEL_BATCHED && p->kernel != GS_KERNEL_PLAIN &&
+         p->kernel != GS_KERNEL_LOCKSTEP)) {
         gs_set_error("gs_params mode out of range");
         return GS_EINVAL;
     }
@@ -363,13 +375,24 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     if (p->kernel == GS_KERNEL_PLAIN) {
         RC(grow(c->hist, c->cap_hist, c->h_small[2] + 1));
         B.hist = c->hist;
-    } else if (p->handoff_lanes >= 0) {
+    } else if (p->kernel == GS_KERNEL_LOCKSTEP && p->handoff_lanes >= 0) {
         B.handoff_lanes = p->handoff_lanes ? p->handoff_lanes : GS_HANDOFF_LANES;
         B.handoff_steps = p->handoff_steps > 0 ? p->handoff_steps : GS_HANDOFF_STEPS;
         if (B.handoff_lanes > 32) B.handoff_lanes = 32;
         RC(grow(c->cont, c->cap_cont, (size_t)n_items * (size_t)B.handoff_lanes + 1));
         B.cont = c->cont;
         B.cont_cap = c->cap_cont;
+    }
+    c->last_walker_cap = 0;
+    if (p->kernel == GS_KERNEL_BATCHED && p->walker_slots >= 0) {
+        /* entries per 16 work items */
+        const uint64_t per16 = p->walker_slots ? (uint64_t)p->walker_slots : 256u;
+        uint64_t want = ((uint64_t)n_items * per16 + 15u) / 16u + 32u;
+        if (want > (1ull << 31)) want = 1ull << 31;   /* 32-bit buffer counter */
+        RC(grow(c->walkers, c->cap_walkers, (size_t)want));
+        B.walkers = c->walkers;
+        B.walker_cap = want;
+        c->last_walker_cap = want;
     }
 
     GS_CUDA(cudaEventRecord(c->ev_s0, st));
@@ -409,6 +432,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     RC(gs_launch_locate(I, B, n_seeds, n_pos, st));
     GS_CUDA(cudaEventRecord(c->ev1, st));
     GS_CUDA(cudaMemcpyAsync(&c->h_small[5], c->queue + 1, 4, cudaMemcpyDeviceToHost, st));
+    GS_CUDA(cudaMemcpyAsync(&c->h_small[10], c->queue + 2, 4, cudaMemcpyDeviceToHost, st));
     if (B.work) GS_CUDA(cudaMemcpyAsync(&c->h_small[6], c->d_work, 32, cudaMemcpyDeviceToHost, st));
     c->n_seeds = n_seeds;
     c->n_pos = n_pos;
@@ -427,6 +451,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     }
     GS_CUDA(cudaStreamSynchronize(st));
     uint32_t flags = (uint32_t)(c->h_small[5] & 0xffffffffu);
+    c->last_walkers = c->last_walker_cap ? (c->h_small[10] & 0xffffffffu) : 0;
     if (B.work) memcpy(c->work, &c->h_small[6], sizeof(c->work));
     cudaEventElapsedTime(&c->t_search, c->ev_s0, c->ev_s1);
     cudaEventElapsedTime(&c->t_total, c->ev0, c->ev1);
@@ -491,12 +516,11 @@ static int enqueue_pass(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     B.slots = c->slots;
     B.slot_cap = c->cap_slots;
     B.item_cap = c->g_items;
-    if (p->handoff_lanes >= 0 && c->cont) {
-        B.handoff_lanes = p->handoff_lanes ? p->handoff_lanes : GS_HANDOFF_LANES;
-        B.handoff_steps = p->handoff_steps > 0 ? p->handoff_steps : GS_HANDOFF_STEPS;
-        if (B.handoff_lanes > 32) B.handoff_lanes = 32;
-        B.cont = c->cont;
-        B.cont_cap = c->cap_cont;
+    /* the walker buffer as the sizing pass left it; walkers beyond it are
+     * walked in the start pass */
+    if (c->last_walker_cap && c->walkers) {
+        B.walkers = c->walkers;
+        B.walker_cap = c->last_walker_cap;
     }
     RC(gs_launch_search(I, B, GS_KERNEL_BATCHED, p->queue_chunk, p->ctas_per_sm, 0, st));
     B.rd_nf = c->rd_nf;
@@ -787,7 +811,10 @@ extern "C" int gs_autotune(gs_ctx *c, const char *d_seqs, const uint64_t *d_offs
         return GS_OK;
     };
     gs_params best = *p;
-    best.kernel = GS_KERNEL_BATCHED;
+    /* the batched search has two knobs (start-pass queue grab, CTAs per
+     * SM); the lockstep form also its two hand-over thresholds */
+    const bool lock = p->kernel == GS_KERNEL_LOCKSTEP;
+    best.kernel = lock ? GS_KERNEL_LOCKSTEP : GS_KERNEL_BATCHED;
     best.count_work = 0;
     if (!best.queue_chunk) best.queue_chunk = GS_QUEUE_CHUNK;
     if (!best.handoff_lanes) best.handoff_lanes = GS_HANDOFF_LANES;
@@ -800,6 +827,7 @@ extern "C" int gs_autotune(gs_ctx *c, const char *d_seqs, const uint64_t *d_offs
     static const int ctas[] = {0, 2, 3, 4};
     for (int round = 0; round < 2; round++) {
         for (int dim = 0; dim < 4; dim++) {
+            if (!lock && (dim == 1 || dim == 2)) continue;
             const int *vals = dim == 0 ? qcs : dim == 1 ? lanes : dim == 2 ? steps : ctas;
             int nv = dim == 0 ? 5 : dim == 1 ? 7 : dim == 2 ? 6 : 4;
             for (int i = 0; i < nv; i++) {

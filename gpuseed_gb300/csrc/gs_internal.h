@@ -48,6 +48,18 @@ struct GsCont {
     uint32_t fwd;
 };
 
+/* A candidate that survived its start in the batched search: its interval
+ * I = [l,u] at far end pos and J = [jl,ju] (jl > ju: none), the interval of
+ * the same string extended by one base toward the longer match (the
+ * neighbour candidate's string at the same far end).  32 bytes. */
+struct __align__(32) GsWalker {
+    uint32_t r;
+    int32_t anchor;     /* bit 31: forward strand */
+    int32_t pos;
+    uint32_t l, u, jl, ju;
+    uint32_t pad;
+};
+
 /* Per-batch device arguments shared by the pipeline kernels. */
 struct GsBatch {
     const char *seqs;          /* ASCII bases */
@@ -76,6 +88,8 @@ struct GsBatch {
     GsCont *cont;              /* NULL: no hand-over; else n_items * handoff_lanes entries */
     int32_t handoff_lanes;     /* hand over when at most this many owned lanes extend ... */
     int32_t handoff_steps;     /* ... after at least this many lockstep steps */
+    GsWalker *walkers;         /* batched search: survivors of the start pass */
+    uint64_t walker_cap;       /* entries allocated (0: every walk stays in the start pass) */
 };
 
 #define GS_FLAG_WALK 1u

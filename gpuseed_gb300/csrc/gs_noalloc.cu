@@ -165,7 +165,8 @@ extern "C" int gs_seed_noalloc(gs_index *idx, const char *d_seqs, const uint64_t
     B.slots = slots;
     B.slot_cap = GS_NOALLOC_MAX_SLOTS;
     B.item_cap = n_items;
-    NA_RC(gs_launch_search(I, B, GS_KERNEL_BATCHED, p->queue_chunk, p->ctas_per_sm, n_items, st));
+    /* the lockstep form: it needs no walker buffer */
+    NA_RC(gs_launch_search(I, B, GS_KERNEL_LOCKSTEP, p->queue_chunk, p->ctas_per_sm, n_items, st));
 
     /* filters and counts; offsets go straight to the caller's arrays */
     B.rd_nf = rd_nf;

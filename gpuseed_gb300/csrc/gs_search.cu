@@ -11,15 +11,20 @@
  * its neighbour toward the longer match (e+1 forward, s-1 reverse) at the
  * same far end: both filters drop such a record, so it need not be produced.
  * The reference prunes with 30 warp shuffles per step over uninitialised
- * flags (:2100-2204); this file uses a defined rule: compare with the nearest
- * still-extending lane to the right, from a GS_HIST-deep own history.
+ * flags (:2100-2204); this file uses a defined rule with three launch forms:
  *
- * Two launch forms:
- *   gs_search_batched: persistent CTAs; each warp takes work items
- *     (read, strand, 31 candidates + 1 helper lane) from a global queue and
- *     steps its 32 candidates in lockstep, one occ lookup per lane per step.
- *   gs_search_plain:   one thread per read, candidates one after another,
- *     containment history in a per-read global array.
+ *   GS_KERNEL_BATCHED (default): gs_search_start + gs_search_walk.  Each
+ *     candidate carries the interval of its neighbour's string at its own
+ *     far end and stops exactly where the rule says; candidates are started
+ *     a warp per work item and walked one per lane (see "batched search").
+ *   GS_KERNEL_LOCKSTEP: gs_search_lockstep + gs_search_tail.  Persistent
+ *     CTAs; each warp takes work items (read, strand, 31 candidates + 1
+ *     helper lane) from a global queue and steps its 32 candidates in
+ *     lockstep, comparing with the nearest still-extending lane to the right
+ *     from a GS_HIST-deep own history; the last candidates of a warp go to a
+ *     tail pass.
+ *   GS_KERNEL_PLAIN: gs_search_plain, one thread per read, candidates one
+ *     after another, containment history in a per-read global array.
  */
 #include "gs_fm.cuh"
 
@@ -138,12 +143,14 @@ int gs_build_kmerx_table(const GsDevIndex &I, uint2 *table, int kx, cudaStream_t
  * base at positions 13..KT-1 takes the 13-mer start and steps over it like
  * the main loop does.  pos = far end reached; alive = interval non-empty;
  * contained (FORCED only) = the start string is always followed by the
- * neighbour's next base (the candidate needs no walk and produces no record). */
+ * neighbour's next base (the candidate needs no walk and produces no record);
+ * fcode = the start table's forced-extension code (0-3, or 4: none/unknown). */
 template <int NSTOP, bool FORCED>
 __device__ __forceinline__ bool gs_start(const GsDevIndex &I, const unsigned char *seq, int anchor,
                                          int dir, bool fwd, int KT, int iL, uint32_t &l,
                                          uint32_t &u, int &pos, bool &alive, bool &contained,
-                                         unsigned long long &w_kmer, unsigned long long &w_blk)
+                                         uint32_t &fcode, unsigned long long &w_kmer,
+                                         unsigned long long &w_blk)
 {
     uint32_t pat = 0;
     int first_bad = KT;
@@ -160,6 +167,7 @@ __device__ __forceinline__ bool gs_start(const GsDevIndex &I, const unsigned cha
     u = 0;
     alive = false;
     contained = false;
+    fcode = 4;
     pos = anchor + dir * (GS_K0 - 1);
     if (first_bad < GS_K0) return false;
     w_kmer++;
@@ -175,6 +183,7 @@ __device__ __forceinline__ bool gs_start(const GsDevIndex &I, const unsigned cha
         uint2 iv = __ldg(&I.kmerx[pat]);
         uint32_t code = iv.y & 7u, size = iv.y >> 3;
         if (code != 7u) {
+            fcode = code;
             l = iv.x;
             u = size ? iv.x + size - 1u : iv.x - 1u;
             pos = anchor + dir * (KT - 1);
@@ -247,13 +256,14 @@ int gs_launch_prepare(GsBatch &b, cudaStream_t st)
 }
 
 /* ------------------------------------------------------------------ */
-/* batched search */
+/* lockstep search */
 
 /* one extension step of a candidate; false when it cannot extend further
  * (read end, empty interval, or a non-ACGT base under GS_N_STOP) */
-template <int NSTOP>
+template <int NSTOP, int COUNT>
 __device__ __forceinline__ bool gs_advance(const GsDevIndex &I, const unsigned char *seq, int iL,
-                                           bool fwd, int dir, uint32_t &l, uint32_t &u, int &pos)
+                                           bool fwd, int dir, uint32_t &l, uint32_t &u, int &pos,
+                                           unsigned long long &w_blk)
 {
     int np = pos + dir;
     if (np < 0 || np >= iL) return false;
@@ -264,7 +274,8 @@ __device__ __forceinline__ bool gs_advance(const GsDevIndex &I, const unsigned c
         return true;
     }
     uint32_t nl = l, nu = u;
-    gs_step(I, nl, nu, c);
+    int blocks = gs_step(I, nl, nu, c);
+    if (COUNT) w_blk += (unsigned long long)blocks;
     if (nl > nu) return false;
     l = nl;
     u = nu;
@@ -298,9 +309,10 @@ __device__ __forceinline__ void gs_write_record(const GsBatch &B, uint32_t r, ui
     else atomicOr(B.queue + 1, GS_FLAG_OVERFLOW);
 }
 
-template <int NSTOP>
-__device__ __forceinline__ void gs_warp_item(const GsDevIndex &I, const GsBatch &B, uint32_t r,
-                                             uint32_t local, int lane)
+template <int NSTOP, int COUNT>
+__device__ __forceinline__ void gs_lockstep_item(const GsDevIndex &I, const GsBatch &B, uint32_t r,
+                                             uint32_t local, int lane, unsigned long long &wk,
+                                             unsigned long long &wb)
 {
     const uint32_t L = B.lengths[r];
     const int k = B.k;
@@ -321,7 +333,6 @@ __device__ __forceinline__ void gs_warp_item(const GsDevIndex &I, const GsBatch 
     uint32_t l = 1, u = 0;
     int pos = anchor;
     bool alive = false, ok = false;
-    unsigned long long wk = 0, wb = 0;
     bool killed = false;
     /* The start table's forced extensions are not used here.  A lockstep warp
      * lasts as long as its longest owned walk; a forced lane dies at step 1
@@ -332,8 +343,9 @@ __device__ __forceinline__ void gs_warp_item(const GsDevIndex &I, const GsBatch 
      * roles, still cost 2.5% of the time (config 3, 10M reads). */
     if (in_range) {
         bool contained = false;
+        uint32_t fcode = 4;
         ok = gs_start<NSTOP, false>(I, seq, anchor, dir, fwd, gs_start_len(I, k), iL, l, u, pos,
-                                    alive, contained, wk, wb);
+                                    alive, contained, fcode, wk, wb);
     }
 
     uint32_t hist[GS_HIST];
@@ -345,7 +357,7 @@ __device__ __forceinline__ void gs_warp_item(const GsDevIndex &I, const GsBatch 
 
     bool pushed = false;
     while (__ballot_sync(0xffffffffu, alive) & owned_mask) {
-        if (alive) alive = gs_advance<NSTOP>(I, seq, iL, fwd, dir, l, u, pos);
+        if (alive) alive = gs_advance<NSTOP, COUNT>(I, seq, iL, fwd, dir, l, u, pos, wb);
         t++;
         uint32_t pub = alive ? u - l + 1u : 0u;
         /* containment: own size d steps ago vs the nearest extending lane
@@ -400,12 +412,28 @@ __device__ __forceinline__ void gs_warp_item(const GsDevIndex &I, const GsBatch 
     if (owned && !pushed) gs_write_record(B, r, n, fwd, anchor, pos, l, u, ok, killed);
 }
 
-/* Tail pass: the candidates handed over by gs_search_batched, one per lane;
+/* executed-work counters (count_work with the batched kernel): a warp sum,
+ * one atomic per warp */
+__device__ __forceinline__ void gs_add_work(const GsBatch &B, unsigned long long wk,
+                                            unsigned long long wb)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        wk += __shfl_xor_sync(0xffffffffu, wk, o);
+        wb += __shfl_xor_sync(0xffffffffu, wb, o);
+    }
+    if ((threadIdx.x & 31) == 0 && B.work) {
+        atomicAdd(&B.work[0], wk);
+        atomicAdd(&B.work[1], wb);
+    }
+}
+
+/* Tail pass: the candidates handed over by gs_search_lockstep, one per lane;
  * a lane takes the next one as soon as its own is finished. */
-template <int NSTOP>
+template <int NSTOP, int COUNT>
 __global__ void __launch_bounds__(256) gs_search_tail(GsDevIndex I, GsBatch B)
 {
     const int lane = threadIdx.x & 31;
+    unsigned long long wb = 0;
     uint32_t n_cont = *(volatile uint32_t *)(B.queue + 2);
     if (n_cont > B.cont_cap) n_cont = (uint32_t)B.cont_cap;
     bool have = false, exhausted = false;
@@ -442,17 +470,19 @@ __global__ void __launch_bounds__(256) gs_search_tail(GsDevIndex I, GsBatch B)
             }
         }
         if (!__ballot_sync(0xffffffffu, have)) break;
-        if (have && !gs_advance<NSTOP>(I, seq, iL, fwd, dir, l, u, pos)) {
+        if (have && !gs_advance<NSTOP, COUNT>(I, seq, iL, fwd, dir, l, u, pos, wb)) {
             gs_write_record(B, r, n, fwd, anchor, pos, l, u, true, false);
             have = false;
         }
     }
+    if (COUNT) gs_add_work(B, 0, wb);
 }
 
-template <int NSTOP>
-__global__ void __launch_bounds__(256, 5) gs_search_batched(GsDevIndex I, GsBatch B, int queue_chunk)
+template <int NSTOP, int COUNT>
+__global__ void __launch_bounds__(256, 5) gs_search_lockstep(GsDevIndex I, GsBatch B, int queue_chunk)
 {
     const int lane = threadIdx.x & 31;
+    unsigned long long wk = 0, wb = 0;
     const uint32_t n_items = B.item_off[B.n_reads];
     if (n_items > B.item_cap) {
         /* the hand-over buffer was sized for fewer items (a captured pass
@@ -475,9 +505,297 @@ __global__ void __launch_bounds__(256, 5) gs_search_batched(GsDevIndex I, GsBatc
         uint32_t r = lo;
         for (uint32_t it = first; it < last; it++) {
             while (B.item_off[r + 1] <= it) r++;
-            gs_warp_item<NSTOP>(I, B, r, it - B.item_off[r], lane);
+            gs_lockstep_item<NSTOP, COUNT>(I, B, r, it - B.item_off[r], lane, wk, wb);
         }
     }
+    if (COUNT) gs_add_work(B, wk, wb);
+}
+
+/* ------------------------------------------------------------------ */
+/* batched search
+ *
+ * Candidate e is contained in e+1 at far end p exactly when
+ * count(R[p..e]) == count(R[p..e+1]) (sizes only fall along the chain
+ * e, e+1, ..., so this is the nearest-extending-candidate rule of the file
+ * comment).  R[p..e+1]'s interval J is nested in R[p..e]'s interval I, so a
+ * candidate can carry J itself and stop at the canonical step without
+ * seeing its neighbour: no lockstep, no helper lane walking, no history.
+ * J's bounds share occurrence blocks with I's whenever I is narrow.
+ *
+ *   gs_search_start: a warp per work item (31 candidates + the next item's
+ *     first, started for its interval only), one round of start-table
+ *     lookups.  The forced-extension code settles J where it can (forced to
+ *     the neighbour's base: contained, stop; forced elsewhere: no J);
+ *     otherwise the walker carries lane+1's start interval and its first
+ *     step in the walk pass extends that to I's far end.  Survivors go to
+ *     the walker buffer in per-warp reserved chunks (unused entries marked
+ *     r = ~0); a walker that finds the buffer full is walked in place.
+ *   gs_search_walk: one walker per lane, each lane refilled as soon as its
+ *     walker ends, from a per-warp window of the buffer. */
+
+#define GS_WALKER_HOLE 0xffffffffu
+#define GS_WALKER_JPEND 1u        /* pad flag: J is one base short of I's far end */
+#define GS_WALKER_CHUNK 512u      /* buffer entries a warp reserves at a time */
+#define GS_WALK_WINDOW 256u       /* buffer entries a walk-pass warp takes at a time */
+
+/* One iteration of a walk: normally a step of I and J with the next
+ * base; for a walker whose J is still one base short (jpend), the J-only
+ * step with the base at pos that brings J to I's far end -- the same call,
+ * so the lanes of a warp take one memory round per iteration either way.
+ * Returns false when the walk is over (killed: it ended by containment). */
+template <int NSTOP, int COUNT>
+__device__ __forceinline__ bool gs_walk_step(const GsDevIndex &I, const unsigned char *seq, int iL,
+                                             bool fwd, int dir, uint32_t &l, uint32_t &u,
+                                             uint32_t &jl, uint32_t &ju, int &pos, bool &jpend,
+                                             bool &killed, unsigned long long &wb)
+{
+    const bool settle = jpend;
+    jpend = false;
+    const int np = settle ? pos : pos + dir;
+    if (np < 0 || np >= iL) return false;
+    const uint32_t c = fwd ? gs_fwd_code(seq[np]) : gs_comp_code(seq[np]);
+    if (c > 3u) {
+        if (!settle) {
+            if (NSTOP) return false;
+            pos = np;   /* wildcard: both intervals unchanged, so no new equality */
+            return true;
+        }
+        /* settle over a wildcard: J unchanged */
+    } else {
+        uint32_t nl = l, nu = u;
+        int blocks = gs_step_pair(I, nl, nu, jl, ju, c, !settle);
+        if (COUNT) wb += (unsigned long long)blocks;
+        if (!settle) {
+            if (nl > nu) return false;   /* natural end at pos */
+            l = nl;
+            u = nu;
+            pos = np;
+        }
+    }
+    if (jl <= ju && ju - jl == u - l) {
+        killed = true;
+        return false;
+    }
+    return true;
+}
+
+/* a walk that did not fit the walker buffer, finished by the start pass
+ * (kept out of line: it is the rare path and would cost the start pass
+ * registers) */
+template <int NSTOP, int COUNT>
+__device__ __noinline__ void gs_walk_in_place(const GsDevIndex &I, const GsBatch &B, uint32_t r,
+                                               uint32_t n, bool fwd, int anchor, int pos,
+                                               uint32_t l, uint32_t u, uint32_t jl, uint32_t ju,
+                                               bool jpend, unsigned long long &wb)
+{
+    const unsigned char *seq = (const unsigned char *)B.seqs + B.offsets[r];
+    const int iL = (int)B.lengths[r];
+    const int dir = fwd ? -1 : 1;
+    bool killed = false;
+    while (gs_walk_step<NSTOP, COUNT>(I, seq, iL, fwd, dir, l, u, jl, ju, pos, jpend, killed, wb)) {
+    }
+    gs_write_record(B, r, n, fwd, anchor, pos, l, u, true, killed);
+}
+
+/* per-warp reservation of walker-buffer entries: [next, end); full once a
+ * reservation came back past the capacity (no further atomics, so the
+ * 32-bit counter cannot wrap) */
+struct GsReserve {
+    uint32_t next, end, full;
+};
+
+template <int NSTOP, int COUNT>
+__device__ __forceinline__ void gs_start_item(const GsDevIndex &I, const GsBatch &B, uint32_t r,
+                                             uint32_t local, int lane, GsReserve &res,
+                                             unsigned long long &wk, unsigned long long &wb)
+{
+    const uint32_t L = B.lengths[r];
+    const int k = B.k;
+    const uint32_t n = L - (uint32_t)k + 1u;
+    const uint32_t nch = (n + GS_CHUNK - 1) / GS_CHUNK;
+    const bool fwd = local < nch;
+    const uint32_t chunk = fwd ? local : local - nch;
+    const uint32_t ci = chunk * GS_CHUNK + (uint32_t)lane;
+    const bool in_range = ci < n;
+    const bool owned = in_range && (lane < GS_CHUNK || ci == n - 1u);
+    const unsigned char *seq = (const unsigned char *)B.seqs + B.offsets[r];
+    const int iL = (int)L;
+    const int anchor = fwd ? (k - 1 + (int)ci) : ((int)n - 1 - (int)ci);
+    const int dir = fwd ? -1 : 1;
+
+    uint32_t l = 1, u = 0, fcode = 4;
+    int pos = anchor;
+    bool alive = false, ok = false, contained = false;
+    if (in_range)
+        ok = gs_start<NSTOP, false>(I, seq, anchor, dir, fwd, gs_start_len(I, k), iL, l, u, pos,
+                                    alive, contained, fcode, wk, wb);
+    /* lane+1 holds the neighbour toward the longer match (e+1 forward, s-1
+     * reverse), started at far end pos - dir */
+    const uint32_t nl = __shfl_down_sync(0xffffffffu, l, 1);
+    const uint32_t nu = __shfl_down_sync(0xffffffffu, u, 1);
+    const int nalive = __shfl_down_sync(0xffffffffu, alive ? 1 : 0, 1);
+
+    bool killed = false, jpend = false;
+    uint32_t jl = 1, ju = 0;
+    if (owned && alive && ci + 1u < n) {
+        const int nb = anchor - dir;
+        const uint32_t cn = fwd ? gs_fwd_code(seq[nb]) : gs_comp_code(seq[nb]);
+        if (cn <= 3u) {
+            if (fcode < 4u) {
+                killed = (fcode == cn);   /* otherwise X·cn does not occur: no J */
+            } else if (nalive) {
+                jl = nl;
+                ju = nu;
+                jpend = true;
+            }
+        }
+        /* cn not ACGT: the candidates to the right never started; this one
+         * walks without J and, if the rule would have stopped it, its record
+         * is one the filters drop */
+    }
+
+    const bool walker = owned && alive && !killed;
+    const uint32_t wm = __ballot_sync(0xffffffffu, walker);
+    if (owned && !walker) gs_write_record(B, r, n, fwd, anchor, pos, l, u, ok, killed);
+    if (!wm) return;
+    /* entries for this item's walkers: the rest of the reservation, then a
+     * new chunk */
+    const uint32_t cnt = (uint32_t)__popc(wm);
+    const uint32_t rank = (uint32_t)__popc(wm & ((1u << lane) - 1u));
+    const uint32_t rem = res.end - res.next;
+    uint32_t g = 0;
+    if (rem < cnt) {
+        if (res.full) {
+            g = (uint32_t)B.walker_cap;
+        } else {
+            if (lane == 0) g = atomicAdd(B.queue + 2, GS_WALKER_CHUNK);
+            g = __shfl_sync(0xffffffffu, g, 0);
+            if ((uint64_t)g + GS_WALKER_CHUNK >= B.walker_cap) res.full = 1u;
+        }
+    }
+    if (walker) {
+        uint64_t idx;
+        if (rank < rem) idx = res.next + rank;
+        else idx = (uint64_t)g + (rank - rem);
+        const uint64_t cap_end = rank < rem ? res.end : min((uint64_t)g + GS_WALKER_CHUNK, B.walker_cap);
+        if (idx < cap_end) {
+            GsWalker w;
+            w.r = r;
+            w.anchor = (int32_t)((uint32_t)anchor | (fwd ? 0x80000000u : 0u));
+            w.pos = pos;
+            w.l = l;
+            w.u = u;
+            w.jl = jl;
+            w.ju = ju;
+            w.pad = jpend ? GS_WALKER_JPEND : 0u;
+            B.walkers[idx] = w;
+        } else {
+            gs_walk_in_place<NSTOP, COUNT>(I, B, r, n, fwd, anchor, pos, l, u, jl, ju, jpend, wb);
+        }
+    }
+    if (rem < cnt) {
+        res.next = (uint32_t)min((uint64_t)g + (cnt - rem), B.walker_cap);
+        res.end = (uint32_t)min((uint64_t)g + GS_WALKER_CHUNK, B.walker_cap);
+        if (res.next > res.end) res.next = res.end;
+    } else {
+        res.next += cnt;
+    }
+}
+
+template <int NSTOP, int COUNT>
+__global__ void __launch_bounds__(256, 3) gs_search_start(GsDevIndex I, GsBatch B, int queue_chunk)
+{
+    const int lane = threadIdx.x & 31;
+    unsigned long long wk = 0, wb = 0;
+    GsReserve res = {0u, 0u, B.walker_cap == 0 ? 1u : 0u};
+    const uint32_t n_items = B.item_off[B.n_reads];
+    for (;;) {
+        uint32_t first = 0;
+        if (lane == 0) first = atomicAdd(B.queue, (uint32_t)queue_chunk);
+        first = __shfl_sync(0xffffffffu, first, 0);
+        if (first >= n_items) break;
+        uint32_t last = min(first + (uint32_t)queue_chunk, n_items);
+        uint32_t lo = 0, hi = B.n_reads;
+        while (lo + 1 < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (B.item_off[mid] <= first) lo = mid; else hi = mid;
+        }
+        uint32_t r = lo;
+        for (uint32_t it = first; it < last; it++) {
+            while (B.item_off[r + 1] <= it) r++;
+            gs_start_item<NSTOP, COUNT>(I, B, r, it - B.item_off[r], lane, res, wk, wb);
+        }
+    }
+    /* unused entries of the last reservation: holes */
+    for (uint32_t i = res.next + (uint32_t)lane; i < res.end; i += 32) B.walkers[i].r = GS_WALKER_HOLE;
+    if (COUNT) gs_add_work(B, wk, wb);
+}
+
+template <int NSTOP, int COUNT>
+__global__ void __launch_bounds__(128) gs_search_walk(GsDevIndex I, GsBatch B)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t lt = (1u << lane) - 1u;
+    unsigned long long wb = 0;
+    uint64_t n_w = *(volatile uint32_t *)(B.queue + 2);
+    if (n_w > B.walker_cap) n_w = B.walker_cap;
+    uint64_t win = 0, win_end = 0;   /* warp-uniform window of walker indices */
+    bool have = false, exhausted = false, killed = false, jpend = false;
+    uint32_t r = 0, l = 0, u = 0, jl = 0, ju = 0, n = 0;
+    int anchor = 0, pos = 0, iL = 0, dir = 0;
+    bool fwd = false;
+    const unsigned char *seq = NULL;
+    for (;;) {
+        uint32_t need = __ballot_sync(0xffffffffu, !have);
+        while (need && !exhausted) {
+            if (win == win_end) {
+                uint32_t g = 0;
+                if (lane == 0) g = atomicAdd(B.queue + 3, GS_WALK_WINDOW);
+                g = __shfl_sync(0xffffffffu, g, 0);
+                if (g >= n_w) {
+                    exhausted = true;
+                    break;
+                }
+                win = g;
+                win_end = min((uint64_t)g + GS_WALK_WINDOW, n_w);
+            }
+            const uint32_t take = (uint32_t)min((uint64_t)__popc(need), win_end - win);
+            const uint32_t rank = __popc(need & lt);
+            if (((need >> lane) & 1u) && rank < take) {
+                GsWalker w = B.walkers[win + rank];
+                if (w.r != GS_WALKER_HOLE) {
+                    r = w.r;
+                    fwd = (w.anchor >> 31) != 0;
+                    anchor = w.anchor & 0x7fffffff;
+                    pos = w.pos;
+                    l = w.l;
+                    u = w.u;
+                    jl = w.jl;
+                    ju = w.ju;
+                    dir = fwd ? -1 : 1;
+                    const uint32_t Lr = B.lengths[r];
+                    iL = (int)Lr;
+                    n = Lr - (uint32_t)B.k + 1u;
+                    seq = (const unsigned char *)B.seqs + B.offsets[r];
+                    have = true;
+                    killed = false;
+                    jpend = (w.pad & GS_WALKER_JPEND) != 0;
+                }
+            }
+            win += take;
+            need = __ballot_sync(0xffffffffu, !have);
+        }
+        if (!__ballot_sync(0xffffffffu, have)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (have &&
+            !gs_walk_step<NSTOP, COUNT>(I, seq, iL, fwd, dir, l, u, jl, ju, pos, jpend, killed, wb)) {
+            gs_write_record(B, r, n, fwd, anchor, pos, l, u, true, killed);
+            have = false;
+        }
+    }
+    if (COUNT) gs_add_work(B, 0, wb);
 }
 
 /* ------------------------------------------------------------------ */
@@ -510,8 +828,9 @@ __global__ void __launch_bounds__(128) gs_search_plain(GsDevIndex I, GsBatch B)
             int pos = anchor;
             bool alive = false;
             bool contained = false;
+            uint32_t fcode = 4;
             bool ok = gs_start<NSTOP, true>(I, seq, anchor, dir, fwd, KT, iL, l, u, pos, alive, contained,
-                                      w_kmer, w_blk);
+                                            fcode, w_kmer, w_blk);
             bool killed = contained;
             if (contained) {
                 /* it reached its start level: the candidates to its left may
@@ -566,10 +885,48 @@ __global__ void __launch_bounds__(128) gs_search_plain(GsDevIndex I, GsBatch B)
 
 /* ------------------------------------------------------------------ */
 
+static int gs_launch_batched(const GsDevIndex &I, GsBatch &B, int queue_chunk, int ctas_per_sm,
+                            uint32_t n_items, cudaStream_t st)
+{
+    int dev = 0, sms = 0;
+    GS_CUDA(cudaGetDevice(&dev));
+    GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (queue_chunk <= 0) queue_chunk = GS_QUEUE_CHUNK;
+    const bool cnt = B.work != NULL, nstop = B.n_mode == GS_N_STOP;
+    void (*start)(GsDevIndex, GsBatch, int) =
+        nstop ? (cnt ? gs_search_start<1, 1> : gs_search_start<1, 0>)
+              : (cnt ? gs_search_start<0, 1> : gs_search_start<0, 0>);
+    void (*walk)(GsDevIndex, GsBatch) = nstop ? (cnt ? gs_search_walk<1, 1> : gs_search_walk<1, 0>)
+                                              : (cnt ? gs_search_walk<0, 1> : gs_search_walk<0, 0>);
+    if (ctas_per_sm <= 0) {
+        int occ = 0;
+        GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, start, 256, 0));
+        ctas_per_sm = occ > 0 ? occ : 1;
+    }
+    uint32_t grid = (uint32_t)sms * (uint32_t)ctas_per_sm;
+    if (n_items) {
+        uint32_t need = (n_items + (uint32_t)queue_chunk - 1) / (uint32_t)queue_chunk;
+        if (need < grid * 8) grid = (need + 7) / 8;
+    }
+    if (grid == 0) grid = 1;
+    GS_CUDA(cudaMemsetAsync(B.queue, 0, sizeof(uint32_t), st));
+    GS_CUDA(cudaMemsetAsync(B.queue + 2, 0, 2 * sizeof(uint32_t), st));
+    start<<<grid, 256, 0, st>>>(I, B, queue_chunk);
+    GS_CUDA(cudaGetLastError());
+    if (B.walker_cap) {
+        int wocc = 0;
+        GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&wocc, walk, 128, 0));
+        walk<<<(uint32_t)sms * (uint32_t)(wocc > 0 ? wocc : 4), 128, 0, st>>>(I, B);
+        GS_CUDA(cudaGetLastError());
+    }
+    return GS_OK;
+}
+
 int gs_launch_search(const GsDevIndex &I, GsBatch &B, int kernel, int queue_chunk, int ctas_per_sm,
                      uint32_t n_items, cudaStream_t st)
 {
     if (B.n_reads == 0) return GS_OK;
+    if (kernel == GS_KERNEL_BATCHED) return gs_launch_batched(I, B, queue_chunk, ctas_per_sm, n_items, st);
     if (kernel == GS_KERNEL_PLAIN) {
         uint32_t nb = (B.n_reads + 127) / 128;
         if (B.n_mode == GS_N_STOP) gs_search_plain<1><<<nb, 128, 0, st>>>(I, B);
@@ -581,12 +938,16 @@ int gs_launch_search(const GsDevIndex &I, GsBatch &B, int kernel, int queue_chun
     GS_CUDA(cudaGetDevice(&dev));
     GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     if (queue_chunk <= 0) queue_chunk = GS_QUEUE_CHUNK;
+    /* count_work: instances that also count the lookups they execute */
+    const bool cnt = B.work != NULL, nstop = B.n_mode == GS_N_STOP;
+    void (*batched)(GsDevIndex, GsBatch, int) =
+        nstop ? (cnt ? gs_search_lockstep<1, 1> : gs_search_lockstep<1, 0>)
+              : (cnt ? gs_search_lockstep<0, 1> : gs_search_lockstep<0, 0>);
+    void (*tail)(GsDevIndex, GsBatch) = nstop ? (cnt ? gs_search_tail<1, 1> : gs_search_tail<1, 0>)
+                                              : (cnt ? gs_search_tail<0, 1> : gs_search_tail<0, 0>);
     if (ctas_per_sm <= 0) {
         int occ = 0;
-        if (B.n_mode == GS_N_STOP)
-            GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gs_search_batched<1>, 256, 0));
-        else
-            GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gs_search_batched<0>, 256, 0));
+        GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched, 256, 0));
         ctas_per_sm = occ > 0 ? occ : 1;
     }
     uint32_t grid = (uint32_t)sms * (uint32_t)ctas_per_sm;
@@ -598,18 +959,13 @@ int gs_launch_search(const GsDevIndex &I, GsBatch &B, int kernel, int queue_chun
     if (grid == 0) grid = 1;
     GS_CUDA(cudaMemsetAsync(B.queue, 0, sizeof(uint32_t), st));
     if (B.cont) GS_CUDA(cudaMemsetAsync(B.queue + 2, 0, 2 * sizeof(uint32_t), st));
-    if (B.n_mode == GS_N_STOP) gs_search_batched<1><<<grid, 256, 0, st>>>(I, B, queue_chunk);
-    else gs_search_batched<0><<<grid, 256, 0, st>>>(I, B, queue_chunk);
+    batched<<<grid, 256, 0, st>>>(I, B, queue_chunk);
     GS_CUDA(cudaGetLastError());
     if (B.cont) {
         int tocc = 0;
-        if (B.n_mode == GS_N_STOP)
-            GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tocc, gs_search_tail<1>, 256, 0));
-        else
-            GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tocc, gs_search_tail<0>, 256, 0));
+        GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tocc, tail, 256, 0));
         uint32_t tgrid = (uint32_t)sms * (uint32_t)(tocc > 0 ? tocc : 4);
-        if (B.n_mode == GS_N_STOP) gs_search_tail<1><<<tgrid, 256, 0, st>>>(I, B);
-        else gs_search_tail<0><<<tgrid, 256, 0, st>>>(I, B);
+        tail<<<tgrid, 256, 0, st>>>(I, B);
         GS_CUDA(cudaGetLastError());
     }
     return GS_OK;

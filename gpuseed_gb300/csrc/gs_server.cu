@@ -54,11 +54,12 @@ struct Req {
 };
 
 /* device bytes one pass needs per base and per read: slots (2 x 16 B per
- * start position), plain-free batched search, hand-over records, per-read
- * counters, outputs (a few seeds and positions per read) */
+ * start position), the batched search's walker buffer (16 entries of 32 B
+ * per work item of 31 start positions, about 33 B per base and 1 KB per
+ * read), per-read counters, outputs (a few seeds and positions per read) */
 inline uint64_t estimate_bytes(uint64_t bases, uint64_t reads)
 {
-    return bases * 40 + reads * 256 + (4u << 20);
+    return bases * 73 + reads * 1280 + (4u << 20);
 }
 
 }  // namespace

@@ -41,8 +41,11 @@ extern "C" {
 #define GS_LF_GPUSEED 0  /* LF(primary+1) = 0 as seed_gen.cu:455-458 */
 #define GS_LF_BWA 1      /* LF as bwa */
 
-#define GS_KERNEL_BATCHED 0 /* warp-cooperative persistent work-queue search */
-#define GS_KERNEL_PLAIN 1   /* one read per thread */
+#define GS_KERNEL_BATCHED 0  /* candidates started a warp per work item, then walked one per
+                                lane, each with its neighbour's interval (default) */
+#define GS_KERNEL_PLAIN 1    /* one read per thread */
+#define GS_KERNEL_LOCKSTEP 2 /* a warp steps 31 candidates in lockstep, comparing neighbours by
+                                shuffles, and hands its last ones to a tail pass */
 
 typedef struct gs_index gs_index;
 typedef struct gs_ctx gs_ctx;
@@ -53,17 +56,19 @@ typedef struct {
     int32_t smem;       /* 1: SMEM mode (-s); 0: MEM mode */
     int32_t n_mode;     /* GS_N_WILDCARD | GS_N_STOP */
     int32_t lf_mode;    /* GS_LF_GPUSEED | GS_LF_BWA */
-    int32_t kernel;     /* GS_KERNEL_BATCHED | GS_KERNEL_PLAIN */
+    int32_t kernel;     /* GS_KERNEL_BATCHED | GS_KERNEL_PLAIN | GS_KERNEL_LOCKSTEP */
     int32_t queue_chunk;    /* work items a warp takes per queue grab (0 = auto) */
     int32_t ctas_per_sm;    /* persistent CTAs per SM (0 = auto) */
     int32_t count_work;     /* 1: count algorithmic work (plain kernel walk + locate) */
-    int32_t handoff_lanes;  /* batched: a warp hands its last extending candidates to a
+    int32_t handoff_lanes;  /* lockstep: a warp hands its last extending candidates to a
                                tail pass once at most this many remain (0 = auto, <0 = never) */
     int32_t handoff_steps;  /* ... but not before this many lockstep steps (0 = auto) */
     int32_t graph;          /* gs_seed_device: 1 = capture the pass into a CUDA graph on the
                                first call and replay it while the inputs (pointers, n_reads,
                                params) repeat; outputs that outgrow the captured capacities
                                fall back to a sized pass and a new capture */
+    int32_t walker_slots;   /* batched: walker buffer entries per 16 work items (0 = auto, 256;
+                               <0 = none: every walk stays in the start pass) */
 } gs_params;
 
 /* One output seed, in output order.  x/y are the reference's int2 read
@@ -154,10 +159,17 @@ void *gs_ctx_stream(gs_ctx *ctx);
 /* Device time (ms) of the last pass's search kernel and of the whole pass,
  * from CUDA events recorded on the context stream. */
 int gs_ctx_last_timing(gs_ctx *ctx, float *search_ms, float *total_ms);
-/* Algorithmic work of the last pass run with count_work = 1 and the plain
- * kernel: 13-mer table lookups, 32-byte occurrence blocks of the
- * containment-stopped walk, LF steps and SA samples of the locate stage. */
+/* Work of the last pass run with count_work = 1: start-table lookups,
+ * 32-byte occurrence blocks of the search, LF steps and SA samples of the
+ * locate stage.  With the plain kernel the search counts are the canonical
+ * containment-stopped walk (the algorithmic work); with the other kernels
+ * they are the lookups those kernels execute. */
 int gs_ctx_last_work(gs_ctx *ctx, uint64_t out[4]);
+
+/* Batched search (GS_KERNEL_BATCHED): candidates of the last call that the
+ * start pass handed to the walk pass, and the walker buffer's capacity
+ * (handed beyond it: walked in the start pass instead). */
+int gs_ctx_last_walkers(gs_ctx *ctx, uint64_t *n_walkers, uint64_t *capacity);
 
 /* ---- autotuner ----------------------------------------------------------
  * Times the batched search on the first `sample` reads (device buffers) over

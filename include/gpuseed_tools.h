@@ -18,6 +18,12 @@ extern "C" {
 int gs_probe_random_gather(int device, uint64_t bytes, uint32_t load_bytes, uint64_t n_loads,
                            double *gbps);
 
+/* The same with 32-byte loads in one of ten load forms: 0 ld.global.nc,
+ * 1 .nc.L1::no_allocate, 2 .cg, 3 .cs, 4 .lu, 5 ld.global, 6 .cv,
+ * 7 .L1::no_allocate, 8 .nc.L1::evict_first, 9 .nc.L2::64B. */
+int gs_probe_random_gather_mode(int device, uint64_t bytes, uint32_t mode, uint64_t n_loads,
+                                double *gbps);
+
 /* Largest L2 fetch from DRAM per miss for this process's context on `device`
  * (cudaLimitMaxL2FetchGranularity: 32, 64 or 128; 0 only reads it).  Returns
  * the value in effect (or a negative GS_E* code).  A context limit: it ends

@@ -40,7 +40,7 @@ def test_config2_subset(built, tmp_path):
     ctx = gs.Context(idx)
     oidx = pyoracle.Index(prefix)
     ob = oidx.seed(seqs, offs, lens, k=19, smem=True)
-    for kernel in (0, 1):
+    for kernel in (0, 1, 2):
         _compare(ctx.seed(seqs, offs, lens, k=19, smem=True, kernel=kernel), ob, lens.size)
     assert any(b"N" in seqs[int(o):int(o) + int(n)].tobytes() for o, n in zip(offs, lens))
 

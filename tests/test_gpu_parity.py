@@ -49,7 +49,7 @@ def test_kmer_table_matches_oracle(small):
     assert np.array_equal(g, o)
 
 
-@pytest.mark.parametrize("kernel", [0, 1], ids=["batched", "plain"])
+@pytest.mark.parametrize("kernel", [0, 1, 2], ids=["batched", "plain", "lockstep"])
 @pytest.mark.parametrize("smem", [False, True], ids=["mem", "smem"])
 @pytest.mark.parametrize("n_mode", [0, 1], ids=["nwild", "nstop"])
 def test_random_reads(small, kernel, smem, n_mode):
@@ -88,7 +88,7 @@ def test_edge_cases(small):
         b"ACGTRYKMSWBDHV@X" * 4,               # other letters (codes 0 and 5)
     ]
     seqs, offs, lens = pack(reads)
-    for kernel in (0, 1):
+    for kernel in (0, 1, 2):
         for smem in (False, True):
             for lf in (0, 1):
                 for k in (13, 20):
@@ -154,7 +154,7 @@ def test_config1_full(built, tmp_path_factory):
     ctx = gs.Context(gidx)
     oidx = pyoracle.Index(prefix)
     ob = oidx.seed(seqs, offs, lens, k=20, smem=False)
-    for kernel in (0, 1):
+    for kernel in (0, 1, 2):
         gres = ctx.seed(seqs, offs, lens, k=20, smem=False, kernel=kernel)
         assert_same(gres, ob, lens.size, f"cfg1 kernel={kernel}")
     assert ob.seeds.shape[0] > 10_000
@@ -187,7 +187,7 @@ def test_longer_start_table(small, kx):
     small["gidx"].set_kmer_len(kx)
     try:
         assert small["gidx"].info().kmer_len == kx
-        for kernel in (0, 1):
+        for kernel in (0, 1, 2):
             for k in (13, kx, kx + 1, 25):
                 for n_mode in (0, 1):
                     for smem in (False, True):
@@ -201,17 +201,53 @@ def test_longer_start_table(small, kx):
 
 @pytest.mark.parametrize("lanes,steps", [(-1, 0), (1, 1), (8, 4), (32, 1), (32, 30)])
 def test_handoff_settings(small, lanes, steps):
-    """The batched search gives the same seeds whether candidates finish in
+    """The lockstep search gives the same seeds whether candidates finish in
     lockstep or are handed to the tail pass, at any threshold."""
     reads = sample_reads(small["codes"], 400, seed=70 + lanes, lengths=(30, 100, 150, 300, 700),
                          err=0.02, n_rate=0.3)
     seqs, offs, lens = pack(reads)
     for smem in (False, True):
         for n_mode in (0, 1):
-            gres = small["ctx"].seed(seqs, offs, lens, k=19, smem=smem, n_mode=n_mode, kernel=0,
+            gres = small["ctx"].seed(seqs, offs, lens, k=19, smem=smem, n_mode=n_mode, kernel=2,
                                      handoff_lanes=lanes, handoff_steps=steps)
             ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=smem, n_mode=n_mode)
             assert_same(gres, ob, len(reads), f"handoff {lanes}/{steps} smem={smem} n={n_mode}")
+
+
+@pytest.mark.parametrize("slots", [-1, 1, 0, 496])
+def test_walker_buffer(small, slots):
+    """The batched search gives the same seeds whether its survivors are walked
+    by the walk pass, by the start pass (no buffer), or split between them
+    (a buffer that overflows)."""
+    reads = sample_reads(small["codes"], 400, seed=80 + slots, lengths=(30, 100, 150, 300, 700),
+                         err=0.02, n_rate=0.3)
+    seqs, offs, lens = pack(reads)
+    for smem in (False, True):
+        for n_mode in (0, 1):
+            ctx = small["ctx"]
+            gres = ctx.seed(seqs, offs, lens, k=19, smem=smem, n_mode=n_mode, kernel=0,
+                            walker_slots=slots)
+            n_w, cap = ctx.last_walkers()
+            assert (cap == 0) == (slots < 0)
+            if slots == 1:
+                assert n_w > cap, "the 1-slot buffer should overflow"
+            ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=smem, n_mode=n_mode)
+            assert_same(gres, ob, len(reads), f"walkers {slots} smem={smem} n={n_mode}")
+
+
+def test_batched_executes_canonical_steps(small):
+    """The batched walk stops every candidate at the canonical step: its
+    executed occurrence blocks stay within a small factor of the canonical
+    count, and no walk runs past a containment (ACGT-only reads)."""
+    reads = sample_reads(small["codes"], 300, seed=33, lengths=(100, 150, 250), err=0.01)
+    seqs, offs, lens = pack(reads)
+    ctx = small["ctx"]
+    ctx.seed(seqs, offs, lens, k=19, smem=True, kernel=1, count_work=True)
+    canon = ctx.last_work()
+    ctx.seed(seqs, offs, lens, k=19, smem=True, kernel=0, count_work=True)
+    batched = ctx.last_work()
+    assert batched["n_kmer"] >= canon["n_kmer"]
+    assert batched["n_occ_blocks"] <= 2 * canon["n_occ_blocks"] + 64
 
 
 def test_graph_replay(small):
