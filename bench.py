@@ -330,6 +330,7 @@ def main():
     ap.add_argument("--ref-step-s", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-text", action="store_true")
     ap.add_argument("--retune", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -518,6 +519,29 @@ def main():
     d2h = int(res.seeds.nbytes + res.pos.nbytes + res.read_seed_off.nbytes + res.read_pos_off.nbytes)
     log(f"[bench] e2e: {e2e_value:,.0f} reads/s")
 
+    # the -o records of this result: GPU formatting vs the host writer, to /dev/null
+    text = None
+    if not args.no_text:
+        fd = os.open(os.devnull, os.O_WRONLY)
+        try:
+            ctx.text_device(1, smem)
+            t0 = time.perf_counter()
+            _, text_bytes = ctx.text_device(1, smem)
+            t_fmt = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            ctx.write_text(fd, 1, smem)
+            t_gpu = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            ctx.write_text(fd, 1, smem, host=True)
+            t_host = time.perf_counter() - t0
+        finally:
+            os.close(fd)
+        text = {"bytes": text_bytes, "gpu_format_ms": t_fmt * 1e3,
+                "gpu_write_ms": t_gpu * 1e3, "host_write_ms": t_host * 1e3,
+                "sink": "/dev/null"}
+        log(f"[bench] -o text {text_bytes / 1e9:.2f} GB: GPU format {t_fmt * 1e3:.1f} ms, "
+            f"GPU format + copy-out + write {t_gpu * 1e3:.1f} ms, host writer {t_host * 1e3:.1f} ms")
+
     latency = None
     if rank == 0 and not args.no_serving:
         latency = serving_sweep(idx, w["codes"], w["nmask"], k, smem, value / ws)
@@ -542,6 +566,7 @@ def main():
             "lockstep": {"search_ms": statistics.mean(lock_ms), "knobs": {"queue_chunk": 16,
                          "handoff_lanes": 2, "handoff_steps": 6}},
             "walkers": {"handed_to_walk_pass": walkers, "buffer": walker_cap},
+            "text": text,
             "work": work,
             "work_executed_batched": {"n_kmer": executed["n_kmer"],
                                       "n_occ_blocks": executed["n_occ_blocks"],

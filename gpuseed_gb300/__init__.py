@@ -28,7 +28,8 @@ GS_ERRORS = {-1: "EINVAL", -2: "EIO", -3: "EFORMAT", -4: "ENOMEM", -5: "ECUDA", 
 EXPORTS = ["gs_index_load", "gs_index_from_host", "gs_index_build", "gs_index_set_kmer_len", "gs_index_free", "gs_index_get_info",
            "gs_index_kmer_table", "gs_index_set_l2_window", "gs_ctx_create", "gs_ctx_free",
            "gs_seed", "gs_seed_device", "gs_result_host", "gs_result_device",
-           "gs_result_write_text", "gs_ctx_stream", "gs_ctx_last_timing", "gs_ctx_last_work",
+           "gs_result_write_text", "gs_result_write_text_host", "gs_result_text_device",
+           "gs_ctx_stream", "gs_ctx_last_timing", "gs_ctx_last_work",
            "gs_ctx_last_walkers",
            "gs_seed_noalloc", "gs_autotune", "gs_server_start", "gs_server_submit", "gs_server_wait",
            "gs_server_result", "gs_server_release", "gs_server_get_stats", "gs_server_stop", "gs_server_replay",
@@ -106,6 +107,8 @@ def lib():
         L.gs_result_host.argtypes = [vp, C.POINTER(ResultView)]
         L.gs_result_device.argtypes = [vp, C.POINTER(ResultView)]
         L.gs_result_write_text.argtypes = [vp, i32, u32, i32]
+        L.gs_result_write_text_host.argtypes = [vp, i32, u32, i32]
+        L.gs_result_text_device.argtypes = [vp, u32, i32, C.POINTER(vp), C.POINTER(u64)]
         L.gs_ctx_stream.argtypes = [vp]
         L.gs_ctx_stream.restype = vp
         L.gs_ctx_last_timing.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
@@ -303,8 +306,17 @@ class Context:
         check(lib().gs_result_device(self.h, C.byref(v)))
         return int(v.n_seeds), int(v.n_pos)
 
-    def write_text(self, fd: int, first_read_no: int = 1, smem: bool = False):
-        check(lib().gs_result_write_text(self.h, fd, first_read_no, 1 if smem else 0))
+    def write_text(self, fd: int, first_read_no: int = 1, smem: bool = False, host=False):
+        """The -o records to an open fd (formatted on the GPU unless host=True)."""
+        f = lib().gs_result_write_text_host if host else lib().gs_result_write_text
+        check(f(self.h, fd, first_read_no, 1 if smem else 0))
+
+    def text_device(self, first_read_no: int = 1, smem: bool = False):
+        """(device pointer, bytes) of the -o records formatted on the GPU."""
+        d, n = C.c_void_p(), C.c_uint64()
+        check(lib().gs_result_text_device(self.h, first_read_no, 1 if smem else 0, C.byref(d),
+                                          C.byref(n)))
+        return int(d.value or 0), int(n.value)
 
     def stream(self) -> int:
         return lib().gs_ctx_stream(self.h) or 0

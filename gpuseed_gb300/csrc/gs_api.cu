@@ -131,7 +131,14 @@ struct gs_ctx {
     uint32_t *pmap; size_t cap_pmap;
     GsCont *cont; size_t cap_cont;
     GsWalker *walkers; size_t cap_walkers;
+    /* text formatting on the GPU */
+    uint32_t *t_sread; size_t cap_t_sread;
+    uint64_t *t_off; size_t cap_t_off;
+    char *t_text; size_t cap_t_text;
+    char *h_text[2];            /* pinned copy-out buffers */
+    cudaEvent_t t_ev[2];
     uint64_t last_walkers, last_walker_cap;
+    uint32_t walker_per16;      /* automatic walker-buffer size, per 16 work items */
     uint32_t *queue;
     uint64_t *d_max;
     unsigned long long *d_work;
@@ -221,6 +228,10 @@ extern "C" void gs_ctx_free(gs_ctx *c)
     cudaFree(c->pos); cudaFree(c->pmap); cudaFree(c->queue); cudaFree(c->d_max);
     cudaFree(c->cont);
     cudaFree(c->walkers);
+    cudaFree(c->t_sread); cudaFree(c->t_off); cudaFree(c->t_text);
+    cudaFreeHost(c->h_text[0]); cudaFreeHost(c->h_text[1]);
+    if (c->t_ev[0]) cudaEventDestroy(c->t_ev[0]);
+    if (c->t_ev[1]) cudaEventDestroy(c->t_ev[1]);
     cudaFree(c->d_work);
     cudaFree(c->cub_tmp);
     cudaFreeHost(c->h_small);
@@ -385,8 +396,11 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     }
     c->last_walker_cap = 0;
     if (p->kernel == GS_KERNEL_BATCHED && p->walker_slots >= 0) {
-        /* entries per 16 work items */
-        const uint64_t per16 = p->walker_slots ? (uint64_t)p->walker_slots : 256u;
+        /* entries per 16 work items: as asked, or automatic -- 16 per item
+         * with a start table (forced codes settle most candidates), all 31
+         * without, and 1.5x more after a pass that filled its buffer */
+        if (!c->walker_per16) c->walker_per16 = I.kx > GS_K0 ? 256u : 512u;
+        const uint64_t per16 = p->walker_slots ? (uint64_t)p->walker_slots : c->walker_per16;
         uint64_t want = ((uint64_t)n_items * per16 + 15u) / 16u + 32u;
         if (want > (1ull << 31)) want = 1ull << 31;   /* 32-bit buffer counter */
         RC(grow(c->walkers, c->cap_walkers, (size_t)want));
@@ -452,6 +466,11 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     GS_CUDA(cudaStreamSynchronize(st));
     uint32_t flags = (uint32_t)(c->h_small[5] & 0xffffffffu);
     c->last_walkers = c->last_walker_cap ? (c->h_small[10] & 0xffffffffu) : 0;
+    if (!p->walker_slots && c->last_walker_cap && c->last_walkers >= c->last_walker_cap &&
+        c->walker_per16 < 512u) {
+        c->walker_per16 += c->walker_per16 / 2;
+        if (c->walker_per16 > 512u) c->walker_per16 = 512u;
+    }
     if (B.work) memcpy(c->work, &c->h_small[6], sizeof(c->work));
     cudaEventElapsedTime(&c->t_search, c->ev_s0, c->ev_s1);
     cudaEventElapsedTime(&c->t_total, c->ev0, c->ev1);
@@ -735,7 +754,7 @@ static inline void ob_u32(OutBuf *o, uint32_t v)
     ob_put(o, t + i, (size_t)(12 - i));
 }
 
-extern "C" int gs_result_write_text(gs_ctx *c, int fd, uint32_t first_read_no, int smem)
+extern "C" int gs_result_write_text_host(gs_ctx *c, int fd, uint32_t first_read_no, int smem)
 {
     if (!c) return GS_EINVAL;
     if (!c->have_host) {
@@ -780,6 +799,117 @@ extern "C" int gs_result_write_text(gs_ctx *c, int fd, uint32_t first_read_no, i
     if (o.err) {
         gs_set_error("write failed");
         return GS_EIO;
+    }
+    return GS_OK;
+}
+
+/* Text records formatted on the GPU from the device result (gs_text.cu):
+ * token lengths, one in-place scan to byte offsets, the bytes. */
+static int format_text_device(gs_ctx *c, uint32_t first_read_no, int smem, uint64_t *n_bytes)
+{
+    if (!c->have_dev) {
+        gs_set_error("no device result to print");
+        return GS_ESTATE;
+    }
+    cudaStream_t st = c->st;
+    const uint64_t n_tok = 2ull * c->n_reads + c->n_seeds + c->n_pos;
+    RC(grow(c->t_sread, c->cap_t_sread, (size_t)c->n_seeds + 1));
+    RC(grow(c->t_off, c->cap_t_off, (size_t)n_tok + 1));
+    GsTextArgs a;
+    memset(&a, 0, sizeof(a));
+    a.n_reads = c->n_reads;
+    a.n_seeds = c->n_seeds;
+    a.n_pos = c->n_pos;
+    a.seed_off = c->seed_off;
+    a.pos_off = c->pos_off;
+    a.seeds = c->seeds;
+    a.seed_pos = c->seed_pos;
+    a.pmap = c->pmap;
+    a.pos = c->pos;
+    a.first_read_no = first_read_no;
+    a.smem = smem ? 1 : 0;
+    a.sread = c->t_sread;
+    a.off = c->t_off;
+    GS_CUDA(cudaMemsetAsync(c->t_off + n_tok, 0, 8, st));
+    RC(gs_launch_text_lengths(a, st));
+    RC(exclusive_scan(c, c->t_off, c->t_off, (size_t)n_tok + 1));
+    GS_CUDA(cudaMemcpyAsync(&c->h_small[11], c->t_off + n_tok, 8, cudaMemcpyDeviceToHost, st));
+    GS_CUDA(cudaStreamSynchronize(st));
+    const uint64_t total = c->h_small[11];
+    RC(grow(c->t_text, c->cap_t_text, (size_t)total + 1));
+    a.text = c->t_text;
+    RC(gs_launch_text_write(a, st));
+    *n_bytes = total;
+    return GS_OK;
+}
+
+extern "C" int gs_result_text_device(gs_ctx *c, uint32_t first_read_no, int smem,
+                                     const char **d_text, uint64_t *n_bytes)
+{
+    if (!c || !d_text || !n_bytes) return GS_EINVAL;
+    uint64_t n = 0;
+    RC(format_text_device(c, first_read_no, smem, &n));
+    GS_CUDA(cudaStreamSynchronize(c->st));
+    *d_text = c->t_text;
+    *n_bytes = n;
+    return GS_OK;
+}
+
+static int write_all(int fd, const char *b, size_t n)
+{
+    size_t off = 0;
+    while (off < n) {
+        ssize_t w = write(fd, b + off, n - off);
+        if (w < 0) {
+            if (errno == EINTR) continue;
+            gs_set_error("write failed: %s", strerror(errno));
+            return GS_EIO;
+        }
+        off += (size_t)w;
+    }
+    return GS_OK;
+}
+
+#define GS_TEXT_CHUNK ((size_t)64 << 20)
+
+/* The -o records: formatted on the GPU when the device result is there,
+ * copied out in 64 MiB chunks through two pinned buffers (the next chunk's
+ * copy overlaps the write of the last); otherwise by the host writer. */
+extern "C" int gs_result_write_text(gs_ctx *c, int fd, uint32_t first_read_no, int smem)
+{
+    if (!c) return GS_EINVAL;
+    if (!c->have_dev) return gs_result_write_text_host(c, fd, first_read_no, smem);
+    uint64_t total = 0;
+    RC(format_text_device(c, first_read_no, smem, &total));
+    for (int i = 0; i < 2; i++) {
+        if (!c->h_text[i]) GS_CUDA(cudaMallocHost(&c->h_text[i], GS_TEXT_CHUNK));
+        if (!c->t_ev[i]) GS_CUDA(cudaEventCreateWithFlags(&c->t_ev[i], cudaEventDisableTiming));
+    }
+    cudaStream_t st = c->st;
+    uint64_t done = 0;
+    int i = 0;
+    if (total) {
+        GS_CUDA(cudaMemcpyAsync(c->h_text[0], c->t_text, (size_t)(total < GS_TEXT_CHUNK ? total : GS_TEXT_CHUNK),
+                                cudaMemcpyDeviceToHost, st));
+        GS_CUDA(cudaEventRecord(c->t_ev[0], st));
+    }
+    while (done < total) {
+        const size_t n = (size_t)(total - done < GS_TEXT_CHUNK ? total - done : GS_TEXT_CHUNK);
+        const uint64_t next = done + n;
+        if (next < total) {
+            const size_t m = (size_t)(total - next < GS_TEXT_CHUNK ? total - next : GS_TEXT_CHUNK);
+            GS_CUDA(cudaMemcpyAsync(c->h_text[(i + 1) & 1], c->t_text + next, m,
+                                    cudaMemcpyDeviceToHost, st));
+            GS_CUDA(cudaEventRecord(c->t_ev[(i + 1) & 1], st));
+        }
+        GS_CUDA(cudaEventSynchronize(c->t_ev[i & 1]));
+        int rc = write_all(fd, c->h_text[i & 1], n);
+        if (rc) {
+            cudaStreamSynchronize(st);
+            return rc;
+        }
+        done = next;
+        i++;
     }
     return GS_OK;
 }

@@ -107,6 +107,21 @@ __host__ __device__ static inline uint32_t gs_comp_code(unsigned char ch)
     return (0x14002035u >> ((ch & 7u) << 2)) & 15u;
 }
 
+/* Device result as the text formatter reads it (gs_text.cu). */
+struct GsTextArgs {
+    uint32_t n_reads;
+    uint64_t n_seeds, n_pos;
+    const uint64_t *seed_off, *pos_off;   /* per read (n+1) */
+    const gs_seed_rec *seeds;
+    const uint64_t *seed_pos;             /* per seed: its first position */
+    const uint32_t *pmap, *pos;           /* per position: its seed, its value */
+    uint32_t first_read_no;
+    int32_t smem;
+    uint32_t *sread;                      /* per seed: its read (written) */
+    uint64_t *off;                        /* per token + 1: lengths, then byte offsets */
+    char *text;
+};
+
 /* host helpers (gs_api.cu) */
 void gs_set_error(const char *fmt, ...);
 int gs_cuda_fail(cudaError_t e, const char *what);
@@ -118,6 +133,8 @@ int gs_cuda_fail(cudaError_t e, const char *what);
 
 /* kernel launchers (defined next to their kernels) */
 int gs_build_kmer_table(const GsDevIndex &idx, uint2 *table, cudaStream_t st);
+int gs_launch_text_lengths(const GsTextArgs &a, cudaStream_t st);
+int gs_launch_text_write(const GsTextArgs &a, cudaStream_t st);
 int gs_build_kmerx_table(const GsDevIndex &idx, uint2 *table, int kx, cudaStream_t st);
 /* n_items: host-known work-item count for grid sizing, or 0 (graph capture):
  * the kernels read the count from item_off[n_reads] on the device */

@@ -152,8 +152,17 @@ int gs_seed_device(gs_ctx *ctx, const char *d_seqs, const uint64_t *d_offsets,
 int gs_result_host(gs_ctx *ctx, gs_result_view *out);
 int gs_result_device(gs_ctx *ctx, gs_result_view *out);
 /* Text records exactly as `seed_gen -o` prints them (seed_gen.cu:3625-3647),
- * appended to an open file descriptor; first_read_no is 1-based. */
+ * appended to an open file descriptor; first_read_no is 1-based.  Formatted
+ * on the GPU from the device result (copied out in 64 MiB chunks that overlap
+ * the writes); by the host from the host result when there is no device
+ * result. */
 int gs_result_write_text(gs_ctx *ctx, int fd, uint32_t first_read_no, int smem);
+/* The same, always formatted by the host from the host result. */
+int gs_result_write_text_host(gs_ctx *ctx, int fd, uint32_t first_read_no, int smem);
+/* The same text in device memory owned by the context (valid until its next
+ * call): *d_text, *n_bytes.  No counterpart in the reference. */
+int gs_result_text_device(gs_ctx *ctx, uint32_t first_read_no, int smem, const char **d_text,
+                          uint64_t *n_bytes);
 /* Stream the context runs on (a cudaStream_t). */
 void *gs_ctx_stream(gs_ctx *ctx);
 /* Device time (ms) of the last pass's search kernel and of the whole pass,

@@ -52,3 +52,23 @@ def pack(reads):
     if len(reads):
         offs[1:] = np.cumsum(lens[:-1], dtype=np.uint64)
     return b"".join(reads), offs, lens
+
+
+def device_bytes(ptr, n):
+    """n bytes of device memory at ptr, copied with the CUDA runtime."""
+    import ctypes
+    import glob
+    if n == 0:
+        return b""
+    rt = None
+    for name in ["libcudart.so"] + sorted(glob.glob("/usr/local/cuda/lib64/libcudart.so*")):
+        try:
+            rt = ctypes.CDLL(name)
+            break
+        except OSError:
+            continue
+    assert rt is not None, "CUDA runtime library not found"
+    rt.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    buf = (ctypes.c_char * n)()
+    assert rt.cudaMemcpy(ctypes.addressof(buf), ptr, n, 2) == 0   # device to host
+    return bytes(buf)

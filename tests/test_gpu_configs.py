@@ -45,6 +45,26 @@ def test_config2_subset(built, tmp_path):
     assert any(b"N" in seqs[int(o):int(o) + int(n)].tobytes() for o, n in zip(offs, lens))
 
 
+def test_config2_text_in_chunks(built, tmp_path):
+    """The GPU-formatted records of a result larger than one 64 MiB copy-out
+    chunk equal the host-formatted ones."""
+    import gpuseed_gb300 as gs
+    from gpuseed_gb300 import workloads as W
+    codes, nmask = W.make_reference(W.ref_spec(2))
+    prefix, idx = _gpu_index(tmp_path, codes, "cfg2t")
+    seqs, offs, lens = W.make_reads(codes, nmask, W.read_spec(2, 400_000))
+    ctx = gs.Context(idx)
+    ctx.seed(seqs, offs, lens, k=19, smem=True)
+    paths = []
+    for host in (False, True):
+        p = tmp_path / f"t{host}.txt"
+        with open(p, "wb") as f:
+            ctx.write_text(f.fileno(), 1, True, host=host)
+        paths.append(p)
+    assert paths[0].stat().st_size > (64 << 20)
+    assert paths[0].read_bytes() == paths[1].read_bytes()
+
+
 def test_config4_long_reads(built, tmp_path):
     import gpuseed_gb300 as gs
     from gpuseed_gb300 import workloads as W

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 import pyoracle
-from helpers import build_index, pack, random_reference, sample_reads
+from helpers import build_index, device_bytes, pack, random_reference, sample_reads
 
 pytestmark = pytest.mark.gpu
 
@@ -112,17 +112,30 @@ def test_invalid_k(small):
 
 
 def test_text_output_identical(small, tmp_path):
+    """The -o records formatted on the GPU, by the host and by the oracle are
+    the same bytes (short reads without seeds, repeats with many positions,
+    read numbers that need every digit width and wrap past 2^32)."""
+    text = "".join("ACGT"[c] for c in small["codes"])
     reads = sample_reads(small["codes"], 300, seed=5, lengths=(50, 100, 150))
+    reads += [b"ACGTACGT", b"A" * 60, text[500:520].encode() * 4, b""]
     seqs, offs, lens = pack(reads)
     for smem in (False, True):
-        small["ctx"].seed(seqs, offs, lens, k=19, smem=smem)
-        gpath = tmp_path / f"g{smem}.txt"
-        with open(gpath, "wb") as f:
-            small["ctx"].write_text(f.fileno(), 1, smem)
-        ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=smem)
-        opath = tmp_path / f"o{smem}.txt"
-        ob.write_text(str(opath), 1, smem)
-        assert gpath.read_bytes() == opath.read_bytes()
+        for first in (1, 9_999_990, 4_294_967_000):
+            small["ctx"].seed(seqs, offs, lens, k=19, smem=smem)
+            outs = []
+            for host in (False, True):
+                path = tmp_path / f"g{smem}{host}.txt"
+                with open(path, "wb") as f:
+                    small["ctx"].write_text(f.fileno(), first, smem, host=host)
+                outs.append(path.read_bytes())
+            d, n = small["ctx"].text_device(first, smem)
+            outs.append(device_bytes(d, n))
+            ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=smem)
+            opath = tmp_path / f"o{smem}.txt"
+            ob.write_text(str(opath), first, smem)
+            want = opath.read_bytes()
+            for i, o in enumerate(outs):
+                assert o == want, (smem, first, i)
 
 
 def test_cli_matches_oracle(small, tmp_path):
