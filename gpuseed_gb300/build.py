@@ -77,7 +77,7 @@ def build(verbose: bool = False) -> str:
         os.replace(tmp, LIB)
     cli_src = os.path.join(CSRC, "seed_gen.c")
     if _stale(CLI, [cli_src, LIB] + headers):
-        _run([cc, "-O2", "-std=gnu11", "-Wall", cli_src, "-o", CLI, "-I", INCLUDE, "-L", PKG,
+        _run([cc, "-O2", "-std=gnu11", "-Wall", "-pthread", cli_src, "-o", CLI, "-I", INCLUDE, "-L", PKG,
               "-lgpuseed", "-Wl,-rpath,$ORIGIN"])
     return LIB
 

@@ -192,7 +192,18 @@ extern "C" int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out)
         gs_ctx_free(c);
         return rc;
     }
+    /* The persisting-L2 carve-out is a limit of the whole CUDA context: once
+     * a context of this process set it, it stays until reset.  On the
+     * search's random accesses it costs time (70.9 -> 94.4 ms on 4M reads of
+     * a 3.1 Gbp index), so a context made with the window off releases it. */
+    static bool persisting_set = false;
     float ratio = gs_index_l2_ratio(idx);
+    if (ratio <= 0.f && persisting_set) {
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+        cudaCtxResetPersistingL2Cache();
+        cudaGetLastError();
+        persisting_set = false;
+    }
     if (ratio > 0.f) {
         int dev = gs_index_device(idx), maxwin = 0, persist = 0;
         cudaDeviceGetAttribute(&maxwin, cudaDevAttrMaxAccessPolicyWindowSize, dev);
@@ -201,6 +212,7 @@ extern "C" int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out)
             size_t occ = gs_index_occ_bytes(idx);
             size_t win = occ < (size_t)maxwin ? occ : (size_t)maxwin;
             cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, (size_t)persist);
+            persisting_set = true;
             cudaStreamAttrValue v;
             memset(&v, 0, sizeof(v));
             v.accessPolicyWindow.base_ptr = (void *)gs_index_dev(idx)->occ;
@@ -353,6 +365,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     B.smem = p->smem ? 1 : 0;
     B.n_mode = p->n_mode;
     B.lf_mode = p->lf_mode;
+    B.max_occ = p->max_occ > 0 ? (uint32_t)p->max_occ : 0u;
     B.queue = c->queue;
     B.work = p->count_work ? c->d_work : NULL;
     memset(c->work, 0, sizeof(c->work));
@@ -523,6 +536,7 @@ static int enqueue_pass(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     B.smem = p->smem ? 1 : 0;
     B.n_mode = p->n_mode;
     B.lf_mode = p->lf_mode;
+    B.max_occ = p->max_occ > 0 ? (uint32_t)p->max_occ : 0u;
     B.queue = c->queue;
     GS_CUDA(cudaMemsetAsync(c->queue, 0, 16, st));
     B.slot_off = c->slot_cnt;

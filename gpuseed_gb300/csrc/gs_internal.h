@@ -88,6 +88,7 @@ struct GsBatch {
     GsCont *cont;              /* NULL: no hand-over; else n_items * handoff_lanes entries */
     int32_t handoff_lanes;     /* hand over when at most this many owned lanes extend ... */
     int32_t handoff_steps;     /* ... after at least this many lockstep steps */
+    uint32_t max_occ;          /* 0 or the largest interval an output seed may have */
     GsWalker *walkers;         /* batched search: survivors of the start pass */
     uint64_t walker_cap;       /* entries allocated (0: every walk stays in the start pass) */
 };

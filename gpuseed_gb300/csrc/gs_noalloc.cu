@@ -141,6 +141,7 @@ extern "C" int gs_seed_noalloc(gs_index *idx, const char *d_seqs, const uint64_t
     B.smem = p->smem ? 1 : 0;
     B.n_mode = p->n_mode;
     B.lf_mode = p->lf_mode;
+    B.max_occ = p->max_occ > 0 ? (uint32_t)p->max_occ : 0u;
     B.queue = queue;
     GS_CUDA(cudaMemsetAsync(queue, 0, 4 * sizeof(uint32_t), st));
 

@@ -34,7 +34,8 @@ __device__ __forceinline__ uint32_t gs_size(const GsRec &r) { return r.u - r.l +
 
 /* decision for forward record o of list F[0..nf) */
 __device__ __forceinline__ void gs_fwd_rule(const GsRec *F, uint32_t nf, uint32_t o, int smem,
-                                            bool &keep, uint32_t &cnt, uint32_t &xl, uint32_t &xu)
+                                            uint32_t max_occ, bool &keep, uint32_t &cnt,
+                                            uint32_t &xl, uint32_t &xu)
 {
     GsRec R = F[o];
     bool same = false;
@@ -55,10 +56,12 @@ __device__ __forceinline__ void gs_fwd_rule(const GsRec *F, uint32_t nf, uint32_
         cnt = sz - nsz;
         if (same) { xl = N.l; xu = N.u; }
     }
+    if (max_occ && sz > max_occ) keep = false;
 }
 
 __device__ __forceinline__ void gs_rev_rule(const GsRec *Rv, uint32_t nr, uint32_t o, int smem,
-                                            bool &keep, uint32_t &cnt, uint32_t &xl, uint32_t &xu)
+                                            uint32_t max_occ, bool &keep, uint32_t &cnt,
+                                            uint32_t &xl, uint32_t &xu)
 {
     (void)nr;
     GsRec R = Rv[o];
@@ -80,6 +83,7 @@ __device__ __forceinline__ void gs_rev_rule(const GsRec *Rv, uint32_t nr, uint32
         cnt = sz - psz;
         if (same) { xl = P.l; xu = P.u; }
     }
+    if (max_occ && sz > max_occ) keep = false;
 }
 
 /* compacts slots[0..n) (y != 0) to the front, in order; returns the count */
@@ -118,12 +122,12 @@ __global__ void __launch_bounds__(256) gs_finalize_count(GsBatch B)
         uint64_t seeds = 0, npos = 0;
         for (uint32_t o = lane; o < nf; o += 32) {
             bool keep; uint32_t cnt, xl, xu;
-            gs_fwd_rule(F, nf, o, B.smem, keep, cnt, xl, xu);
+            gs_fwd_rule(F, nf, o, B.smem, B.max_occ, keep, cnt, xl, xu);
             if (keep && cnt) { seeds++; npos += cnt; }
         }
         for (uint32_t o = lane; o < nr; o += 32) {
             bool keep; uint32_t cnt, xl, xu;
-            gs_rev_rule(Rv, nr, o, B.smem, keep, cnt, xl, xu);
+            gs_rev_rule(Rv, nr, o, B.smem, B.max_occ, keep, cnt, xl, xu);
             if (keep && cnt) { seeds++; npos += cnt; }
         }
         for (int off = 16; off; off >>= 1) {
@@ -159,10 +163,10 @@ __global__ void __launch_bounds__(128) gs_finalize_emit(GsBatch B, uint64_t *see
         bool keep; uint32_t cnt, xl, xu;
         GsRec R;
         if (take_f) {
-            gs_fwd_rule(F, nf, a, B.smem, keep, cnt, xl, xu);
+            gs_fwd_rule(F, nf, a, B.smem, B.max_occ, keep, cnt, xl, xu);
             R = F[a++];
         } else {
-            gs_rev_rule(Rv, nr, b, B.smem, keep, cnt, xl, xu);
+            gs_rev_rule(Rv, nr, b, B.smem, B.max_occ, keep, cnt, xl, xu);
             R = Rv[b++];
         }
         if (keep && cnt) {

@@ -7,14 +7,17 @@
  * the same stdout records (seed_gen.cu:3625-3647).  FASTA handling follows
  * the reference's getline loop (seed_gen.cu:2955-2990): lines starting with
  * '>' are skipped, every other line is one read whose last character (the
- * newline) is dropped.  Reads are processed in batches of at least
- * BATCH_BASES bases, numbered from 1 across batches.
+ * newline) is dropped.  Reads are processed in batches of at least -B bases
+ * (64 Mi by default), numbered from 1 across batches; a reader thread parses
+ * the next batch while the GPU seeds the current one and its records are
+ * printed (formatted on the GPU).
  *
  * Extra options, off by default: -n (a non-ACGT base stops the extension),
  * -b (bwa's LF at row primary+1), -P (one-read-per-thread search kernel),
  * -B INT (bases per batch), -F (record-aware input: FASTA records over several
  * lines, FASTQ, CR LF line ends, a .gz file read through `gzip -dc`; a last
- * line without a newline keeps its last base).  Errors print a message and
+ * line without a newline keeps its last base), -c INT (drop seeds that occur
+ * more than INT times, as bwa's -c).  Errors print a message and
  * exit with status 1, as the reference does for unreadable index files.
  */
 #define _GNU_SOURCE
@@ -23,6 +26,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <sys/time.h>
+#include <pthread.h>
 #include <unistd.h>
 
 #include "../../include/gpuseed.h"
@@ -89,6 +93,114 @@ static void die(const char *what, int rc)
     exit(1);
 }
 
+/* One batch of reads as the reader thread fills it. */
+typedef struct {
+    char *bases;
+    uint64_t *offs;
+    uint32_t *lens;
+    size_t cap_b, cap_r;
+    uint64_t nb;
+    uint32_t nr;
+    int ready;   /* filled and waiting for the GPU */
+    int last;    /* the input ends with this batch */
+    int err;     /* out of host memory */
+} batch_t;
+
+/* The reader thread parses batch i+1 while the GPU seeds batch i and its
+ * records are printed: two batches, handed back and forth. */
+typedef struct {
+    FILE *fp;
+    int records;
+    uint64_t batch_bases;
+    batch_t b[2];
+    pthread_mutex_t mu;
+    pthread_cond_t cv;
+    char *line, *rec;
+    size_t line_cap, rec_cap;
+    int pending_header;
+    double t_load;
+} reader_t;
+
+static void fill_batch(reader_t *R, batch_t *B)
+{
+    B->nb = 0;
+    B->nr = 0;
+    B->last = 0;
+    B->err = 0;
+    while (B->nb < R->batch_bases) {
+        const char *src;
+        size_t L;
+        if (R->records) {
+            ssize_t n = next_record(R->fp, &R->line, &R->line_cap, &R->rec, &R->rec_cap,
+                                    &R->pending_header);
+            if (n < 0) {
+                B->last = 1;
+                break;
+            }
+            src = R->rec;
+            L = (size_t)n;
+        } else {
+            ssize_t n = getline(&R->line, &R->line_cap, R->fp);
+            if (n < 0) {
+                B->last = 1;
+                break;
+            }
+            if (R->line[0] == '>') continue;
+            src = R->line;
+            L = n > 0 ? (size_t)n - 1 : 0;
+        }
+        if (B->nb + L + 1 > B->cap_b) {
+            size_t cap = B->cap_b ? B->cap_b : (1u << 20);
+            while (B->nb + L + 1 > cap) cap *= 2;
+            char *nbuf = (char *)realloc(B->bases, cap);
+            if (!nbuf) {
+                B->err = 1;
+                return;
+            }
+            B->bases = nbuf;
+            B->cap_b = cap;
+        }
+        if (B->nr + 1 > B->cap_r) {
+            size_t cap = B->cap_r ? 2 * B->cap_r : (1u << 16);
+            uint64_t *no = (uint64_t *)realloc(B->offs, cap * 8);
+            if (no) B->offs = no;
+            uint32_t *nl = (uint32_t *)realloc(B->lens, cap * 4);
+            if (nl) B->lens = nl;
+            if (!no || !nl) {
+                B->err = 1;
+                return;
+            }
+            B->cap_r = cap;
+        }
+        memcpy(B->bases + B->nb, src, L);
+        B->offs[B->nr] = B->nb;
+        B->lens[B->nr] = (uint32_t)L;
+        B->nb += L;
+        B->nr++;
+    }
+}
+
+static void *reader_main(void *arg)
+{
+    reader_t *R = (reader_t *)arg;
+    for (int i = 0;; i ^= 1) {
+        batch_t *B = &R->b[i];
+        pthread_mutex_lock(&R->mu);
+        while (B->ready) pthread_cond_wait(&R->cv, &R->mu);
+        pthread_mutex_unlock(&R->mu);
+        double t0 = now_s();
+        fill_batch(R, B);
+        R->t_load += now_s() - t0;
+        int stop = B->last || B->err;
+        pthread_mutex_lock(&R->mu);
+        B->ready = 1;
+        pthread_cond_broadcast(&R->cv);
+        pthread_mutex_unlock(&R->mu);
+        if (stop) break;
+    }
+    return NULL;
+}
+
 int main(int argc, char *argv[])
 {
     double t_start = now_s();
@@ -97,7 +209,7 @@ int main(int argc, char *argv[])
     p.k = 20;
     uint64_t batch_bases = 64u << 20;
     int print_out = 0, records = 0, c;
-    while ((c = getopt(argc, argv, "k:sonbPB:F")) >= 0) {
+    while ((c = getopt(argc, argv, "k:sonbPB:Fc:")) >= 0) {
         switch (c) {
         case 'k': p.k = atoi(optarg); break;
         case 's': p.smem = 1; break;
@@ -107,6 +219,7 @@ int main(int argc, char *argv[])
         case 'P': p.kernel = GS_KERNEL_PLAIN; break;
         case 'B': batch_bases = strtoull(optarg, NULL, 10); break;
         case 'F': records = 1; break;
+        case 'c': p.max_occ = atoi(optarg); break;
         default: break;
         }
     }
@@ -115,6 +228,7 @@ int main(int argc, char *argv[])
                         "<reads fasta file>\n");
         return 1;
     }
+    if (batch_bases == 0) batch_bases = 1;
     fprintf(stderr, "Loading index from file and copying it to GPU...\n");
     double t0 = now_s();
     gs_index *idx = NULL;
@@ -144,89 +258,69 @@ int main(int argc, char *argv[])
         fprintf(stderr, "seed_gen: cannot open %s\n", argv[optind + 1]);
         return 1;
     }
-    size_t cap_b = 1 << 20, cap_r = 1 << 16;
-    char *bases = (char *)malloc(cap_b);
-    uint64_t *offs = (uint64_t *)malloc(cap_r * 8);
-    uint32_t *lens = (uint32_t *)malloc(cap_r * 4);
-    char *line = NULL, *rec = NULL;
-    size_t line_cap = 0, rec_cap = 0;
-    int pending_header = 0;
-    uint32_t reads_done = 0;
-    double t_gpu = 0, t_load = 0, t_print = 0;
-    int all_done = 0;
-    while (!all_done) {
-        double tl = now_s();
-        uint64_t nb = 0;
-        uint32_t nr = 0;
-        while (nb < batch_bases) {
-            const char *src;
-            size_t L;
-            if (records) {
-                ssize_t n = next_record(fp, &line, &line_cap, &rec, &rec_cap, &pending_header);
-                if (n < 0) {
-                    all_done = 1;
-                    break;
-                }
-                src = rec;
-                L = (size_t)n;
-            } else {
-                ssize_t n = getline(&line, &line_cap, fp);
-                if (n < 0) {
-                    all_done = 1;
-                    break;
-                }
-                if (line[0] == '>') continue;
-                src = line;
-                L = n > 0 ? (size_t)n - 1 : 0;
-            }
-            if (nb + L + 1 > cap_b) {
-                while (nb + L + 1 > cap_b) cap_b *= 2;
-                bases = (char *)realloc(bases, cap_b);
-            }
-            if (nr + 1 > cap_r) {
-                cap_r *= 2;
-                offs = (uint64_t *)realloc(offs, cap_r * 8);
-                lens = (uint32_t *)realloc(lens, cap_r * 4);
-            }
-            if (!bases || !offs || !lens) {
-                fprintf(stderr, "seed_gen: out of host memory\n");
-                return 1;
-            }
-            memcpy(bases + nb, src, L);
-            offs[nr] = nb;
-            lens[nr] = (uint32_t)L;
-            nb += L;
-            nr++;
-        }
-        t_load += now_s() - tl;
-        if (nr == 0) break;
-        double tg = now_s();
-        rc = gs_seed(ctx, bases, offs, lens, nr, &p);
-        if (rc) die("seeding batch", rc);
-        t_gpu += now_s() - tg;
-        gs_result_view v;
-        gs_result_host(ctx, &v);
-        fprintf(stderr, "batch of %u reads: %llu seeds, %llu positions, %.3f s on GPU\n", nr,
-                (unsigned long long)v.n_seeds, (unsigned long long)v.n_pos, now_s() - tg);
-        if (print_out) {
-            double tp = now_s();
-            fflush(stdout);
-            rc = gs_result_write_text(ctx, 1, reads_done + 1, p.smem);
-            if (rc) die("writing records", rc);
-            t_print += now_s() - tp;
-        }
-        reads_done += nr;
+    reader_t R;
+    memset(&R, 0, sizeof(R));
+    R.fp = fp;
+    R.records = records;
+    R.batch_bases = batch_bases;
+    pthread_mutex_init(&R.mu, NULL);
+    pthread_cond_init(&R.cv, NULL);
+    pthread_t reader;
+    if (pthread_create(&reader, NULL, reader_main, &R) != 0) {
+        fprintf(stderr, "seed_gen: cannot start the reader thread\n");
+        return 1;
     }
+    uint32_t reads_done = 0;
+    double t_gpu = 0, t_print = 0;
+    for (int i = 0;; i ^= 1) {
+        batch_t *B = &R.b[i];
+        pthread_mutex_lock(&R.mu);
+        while (!B->ready) pthread_cond_wait(&R.cv, &R.mu);
+        pthread_mutex_unlock(&R.mu);
+        if (B->err) {
+            fprintf(stderr, "seed_gen: out of host memory\n");
+            return 1;
+        }
+        const int last = B->last;
+        if (B->nr) {
+            double tg = now_s();
+            rc = gs_seed(ctx, B->bases, B->offs, B->lens, B->nr, &p);
+            if (rc) die("seeding batch", rc);
+            t_gpu += now_s() - tg;
+            gs_result_view v;
+            gs_result_host(ctx, &v);
+            fprintf(stderr, "batch of %u reads: %llu seeds, %llu positions, %.3f s on GPU\n", B->nr,
+                    (unsigned long long)v.n_seeds, (unsigned long long)v.n_pos, now_s() - tg);
+            if (print_out) {
+                double tp = now_s();
+                fflush(stdout);
+                rc = gs_result_write_text(ctx, 1, reads_done + 1, p.smem);
+                if (rc) die("writing records", rc);
+                t_print += now_s() - tp;
+            }
+            reads_done += B->nr;
+        }
+        pthread_mutex_lock(&R.mu);
+        B->ready = 0;
+        pthread_cond_broadcast(&R.cv);
+        pthread_mutex_unlock(&R.mu);
+        if (last) break;
+    }
+    pthread_join(reader, NULL);
     if (piped) pclose(fp);
     else fclose(fp);
-    free(line);
-    free(rec);
-    free(bases);
-    free(offs);
-    free(lens);
+    free(R.line);
+    free(R.rec);
+    for (int i = 0; i < 2; i++) {
+        free(R.b[i].bases);
+        free(R.b[i].offs);
+        free(R.b[i].lens);
+    }
     gs_ctx_free(ctx);
     gs_index_free(idx);
-    fprintf(stderr, "%s seeds: %u reads, GPU time %.3f s, load %.3f s, print %.3f s, total %.3f s\n",
-            p.smem ? "SMEM" : "MEM", reads_done, t_gpu, t_load, t_print, now_s() - t_start);
+    fprintf(stderr,
+            "%s seeds: %u reads, GPU time %.3f s, load %.3f s (overlapped), print %.3f s, total "
+            "%.3f s\n",
+            p.smem ? "SMEM" : "MEM", reads_done, t_gpu, R.t_load, t_print, now_s() - t_start);
     return 0;
 }

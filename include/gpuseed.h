@@ -69,6 +69,9 @@ typedef struct {
                                fall back to a sized pass and a new capture */
     int32_t walker_slots;   /* batched: walker buffer entries per 16 work items (0 = auto, 256;
                                <0 = none: every walk stays in the start pass) */
+    int32_t max_occ;        /* > 0: drop output seeds whose interval has more rows than this
+                               (bwa's -c; applied after the filters, the other seeds are
+                               unchanged); 0 = off, the reference's output */
 } gs_params;
 
 /* One output seed, in output order.  x/y are the reference's int2 read
@@ -130,8 +133,11 @@ int gs_index_build(const uint8_t *codes, uint64_t n, uint32_t sa_intv, int devic
  * SA interval of a string does not depend on how it is found, so results do
  * not change; seeding uses it only when k > len. */
 int gs_index_set_kmer_len(gs_index *idx, int kmer_len);
-/* Keeps the occurrence table in L2 under an access-policy window on every
- * context stream (fraction of the set-aside, 0 disables). */
+/* Keeps the occurrence table in L2 under an access-policy window on the
+ * streams of contexts created afterwards (fraction of the set-aside; 0, the
+ * default, disables it and releases the set-aside).  Measured slower on the
+ * search's random accesses (70.9 -> 94.4 ms, 4M reads on 3.1 Gbp): off
+ * unless asked for. */
 int gs_index_set_l2_window(gs_index *idx, float hit_ratio);
 
 /* ---- seeding context ---------------------------------------------------

@@ -147,12 +147,21 @@ def test_cli_matches_oracle(small, tmp_path):
             f.write(b">r%d\n%s\n" % (i, r))
     seqs, offs, lens = pack(reads)
     for smem in (False, True):
-        args = [gs.CLI_PATH, "-k", "19"] + (["-s"] if smem else []) + ["-o", small["prefix"], str(fa)]
-        out = subprocess.run(args, capture_output=True, check=True).stdout
         ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=smem)
         opath = tmp_path / "o.txt"
         ob.write_text(str(opath), 1, smem)
-        assert out == opath.read_bytes()
+        # default batch, and batches of one read, ~10 reads, ~70 reads (the
+        # reader thread parses the next batch while one is seeded)
+        for batch in ([], ["-B", "1"], ["-B", "1000"], ["-B", "7000"]):
+            args = ([gs.CLI_PATH, "-k", "19"] + (["-s"] if smem else []) + batch +
+                    ["-o", small["prefix"], str(fa)])
+            out = subprocess.run(args, capture_output=True, check=True).stdout
+            assert out == opath.read_bytes(), batch
+    empty = tmp_path / "empty.fa"
+    empty.write_bytes(b">only a header\n")
+    out = subprocess.run([gs.CLI_PATH, "-k", "19", "-o", small["prefix"], str(empty)],
+                         capture_output=True, check=True).stdout
+    assert out == b""
 
 
 def test_config1_full(built, tmp_path_factory):
@@ -261,6 +270,28 @@ def test_batched_executes_canonical_steps(small):
     batched = ctx.last_work()
     assert batched["n_kmer"] >= canon["n_kmer"]
     assert batched["n_occ_blocks"] <= 2 * canon["n_occ_blocks"] + 64
+
+
+@pytest.mark.parametrize("kernel", [0, 1])
+def test_max_occ_cap(small, kernel):
+    """max_occ drops exactly the output seeds whose interval is larger than
+    the cap and leaves the others (and their positions) as they were."""
+    codes = small["codes"]
+    text = "".join("ACGT"[c] for c in codes)
+    reads = sample_reads(codes, 300, seed=44, lengths=(50, 100, 150), err=0.02)
+    reads += [text[500:530].encode() * 3, b"ACGT" * 20]
+    seqs, offs, lens = pack(reads)
+    for smem in (False, True):
+        ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=smem)
+        for cap in (1, 2, 5):
+            gres = small["ctx"].seed(seqs, offs, lens, k=19, smem=smem, kernel=kernel, max_occ=cap)
+            dropped = 0
+            for r in range(len(reads)):
+                want = [rec for rec in ob.read_records(r) if rec[3] - rec[2] + 1 <= cap]
+                dropped += len(ob.read_records(r)) - len(want)
+                assert gres.read_records(r) == want, (smem, cap, r)
+            if cap == 1:
+                assert dropped > 0
 
 
 def test_graph_replay(small):
