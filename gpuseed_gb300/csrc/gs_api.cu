@@ -124,6 +124,7 @@ struct gs_ctx {
     uint64_t *seed_off, *pos_off; size_t cap_so, cap_po;
     /* per candidate / base / output */
     GsRec *slots; size_t cap_slots;
+    uint32_t *recmask; size_t cap_recmask;
     uint32_t *hist; size_t cap_hist;
     gs_seed_rec *seeds; size_t cap_seeds;
     uint64_t *seed_pos; size_t cap_seed_pos;
@@ -240,6 +241,7 @@ extern "C" void gs_ctx_free(gs_ctx *c)
     cudaFree(c->pos); cudaFree(c->pmap); cudaFree(c->queue); cudaFree(c->d_max);
     cudaFree(c->cont);
     cudaFree(c->walkers);
+    cudaFree(c->recmask);
     cudaFree(c->t_sread); cudaFree(c->t_off); cudaFree(c->t_text);
     cudaFreeHost(c->h_text[0]); cudaFreeHost(c->h_text[1]);
     if (c->t_ev[0]) cudaEventDestroy(c->t_ev[0]);
@@ -393,8 +395,11 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     uint64_t n_slots = c->h_small[0];
     uint32_t n_items = (uint32_t)(c->h_small[1] & 0xffffffffu);
     RC(grow(c->slots, c->cap_slots, n_slots + 1));
+    RC(grow(c->recmask, c->cap_recmask, (c->cap_slots + 31) / 32 + 1));
     B.slots = c->slots;
     B.slot_cap = c->cap_slots;
+    B.recmask = c->recmask;
+    GS_CUDA(cudaMemsetAsync(c->recmask, 0, ((n_slots + 31) / 32 + 1) * sizeof(uint32_t), st));
     B.item_cap = n_items;
     if (p->kernel == GS_KERNEL_PLAIN) {
         RC(grow(c->hist, c->cap_hist, c->h_small[2] + 1));
@@ -548,6 +553,8 @@ static int enqueue_pass(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     B.item_off = c->item_off;
     B.slots = c->slots;
     B.slot_cap = c->cap_slots;
+    B.recmask = c->recmask;
+    GS_CUDA(cudaMemsetAsync(c->recmask, 0, ((c->cap_slots + 31) / 32 + 1) * sizeof(uint32_t), st));
     B.item_cap = c->g_items;
     /* the walker buffer as the sizing pass left it; walkers beyond it are
      * walked in the start pass */

@@ -69,7 +69,8 @@ struct GsBatch {
     int32_t k, smem, n_mode, lf_mode;
     uint64_t *slot_off;        /* per read (n+1): first candidate slot */
     uint32_t *item_off;        /* per read (n+1): first work item */
-    GsRec *slots;              /* 2 * candidates */
+    GsRec *slots;              /* 2 * candidates; only slots holding a record are written */
+    uint32_t *recmask;         /* one bit per slot: the slot holds a record (zeroed per pass) */
     uint32_t *hist;            /* plain kernel: one word per base */
     uint32_t *rd_nf, *rd_nr;   /* per read: compacted record counts */
     uint64_t *rd_nseeds, *rd_npos;   /* per read counts ... */

@@ -122,10 +122,11 @@ extern "C" int gs_seed_noalloc(gs_index *idx, const char *d_seqs, const uint64_t
     if (b2 > cub_bytes) cub_bytes = b2;
     unsigned char *cub_tmp = cv.take<unsigned char>(cub_bytes + 256);
     GsRec *slots = cv.take<GsRec>(GS_NOALLOC_MAX_SLOTS);
+    uint32_t *recmask = cv.take<uint32_t>(GS_NOALLOC_MAX_SLOTS / 32 + 1);
     uint64_t *seed_pos = cv.take<uint64_t>(GS_NOALLOC_MAX_SEEDS);
     uint32_t *pmap = cv.take<uint32_t>(GS_NOALLOC_MAX_POS);
     if (!slot_cnt || !slot_off || !item_cnt || !item_off || !rd_nf || !rd_nr || !rd_nseeds ||
-        !rd_npos || !queue || !cub_tmp || !slots || !seed_pos || !pmap) {
+        !rd_npos || !queue || !cub_tmp || !slots || !recmask || !seed_pos || !pmap) {
         gs_set_error("gs_seed_noalloc: scratch layout exceeds %u bytes",
                      (unsigned)GS_NOALLOC_SCRATCH_BYTES);
         return GS_ENOMEM;
@@ -165,6 +166,8 @@ extern "C" int gs_seed_noalloc(gs_index *idx, const char *d_seqs, const uint64_t
     B.item_off = item_off;
     B.slots = slots;
     B.slot_cap = GS_NOALLOC_MAX_SLOTS;
+    B.recmask = recmask;
+    GS_CUDA(cudaMemsetAsync(recmask, 0, ((n_slots + 31) / 32 + 1) * sizeof(uint32_t), st));
     B.item_cap = n_items;
     /* the lockstep form: it needs no walker buffer */
     NA_RC(gs_launch_search(I, B, GS_KERNEL_LOCKSTEP, p->queue_chunk, p->ctas_per_sm, n_items, st));

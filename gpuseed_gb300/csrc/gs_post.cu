@@ -86,21 +86,25 @@ __device__ __forceinline__ void gs_rev_rule(const GsRec *Rv, uint32_t nr, uint32
     if (max_occ && sz > max_occ) keep = false;
 }
 
-/* compacts slots[0..n) (y != 0) to the front, in order; returns the count */
-__device__ __forceinline__ uint32_t gs_warp_compact(GsRec *s, uint32_t n, int lane)
+/* compacts the records among slots s0..s0+n (flagged in the record mask;
+ * the other slots were never written) to the front, in order; returns the
+ * count.  Only flagged slots are read. */
+__device__ __forceinline__ uint32_t gs_warp_compact(GsRec *slots, const uint32_t *mask, uint64_t s0,
+                                                    uint32_t n, int lane)
 {
     uint32_t cnt = 0;
     for (uint32_t c0 = 0; c0 < n; c0 += 32) {
-        uint32_t i = c0 + (uint32_t)lane;
+        const uint32_t i = c0 + (uint32_t)lane;
         GsRec r;
         bool v = false;
         if (i < n) {
-            r = s[i];
-            v = r.y != 0;
+            const uint64_t g = s0 + i;
+            v = (mask[g >> 5] >> (g & 31u)) & 1u;
+            if (v) r = slots[g];
         }
         uint32_t m = __ballot_sync(0xffffffffu, v);
         __syncwarp();
-        if (v) s[cnt + __popc(m & ((1u << lane) - 1u))] = r;
+        if (v) slots[s0 + cnt + __popc(m & ((1u << lane) - 1u))] = r;
         __syncwarp();
         cnt += __popc(m);
     }
@@ -114,11 +118,23 @@ __global__ void __launch_bounds__(256) gs_finalize_count(GsBatch B)
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t r = warp; r < B.n_reads; r += nwarps) {
         uint64_t base = B.slot_off[r];
+        if (B.slot_off[r + 1] > B.slot_cap) {
+            /* a replayed pass whose input needs more slots than it was sized
+             * for: nothing of this read is there; the host re-sizes */
+            if (lane == 0) {
+                B.rd_nf[r] = 0;
+                B.rd_nr[r] = 0;
+                B.rd_nseeds[r] = 0;
+                B.rd_npos[r] = 0;
+                atomicOr(B.queue + 1, GS_FLAG_OVERFLOW);
+            }
+            continue;
+        }
         uint32_t n = (uint32_t)((B.slot_off[r + 1] - base) >> 1);
         GsRec *F = B.slots + base;
         GsRec *Rv = F + n;
-        uint32_t nf = gs_warp_compact(F, n, lane);
-        uint32_t nr = gs_warp_compact(Rv, n, lane);
+        uint32_t nf = gs_warp_compact(B.slots, B.recmask, base, n, lane);
+        uint32_t nr = gs_warp_compact(B.slots, B.recmask, base + n, n, lane);
         uint64_t seeds = 0, npos = 0;
         for (uint32_t o = lane; o < nf; o += 32) {
             bool keep; uint32_t cnt, xl, xu;

@@ -304,9 +304,14 @@ __device__ __forceinline__ void gs_write_record(const GsBatch &B, uint32_t r, ui
             rec.y = (int32_t)((uint32_t)(pos + 1) | 0x80000000u);
         }
     }
+    if (rec.y == 0) return;   /* no record: the slot stays unflagged and unwritten */
     uint64_t slot = B.slot_off[r] + (fwd ? (uint64_t)(anchor - (k - 1)) : (uint64_t)n + (uint64_t)anchor);
-    if (slot < B.slot_cap) B.slots[slot] = rec;
-    else atomicOr(B.queue + 1, GS_FLAG_OVERFLOW);
+    if (slot < B.slot_cap) {
+        B.slots[slot] = rec;
+        atomicOr(B.recmask + (slot >> 5), 1u << (slot & 31u));
+    } else {
+        atomicOr(B.queue + 1, GS_FLAG_OVERFLOW);
+    }
 }
 
 template <int NSTOP, int COUNT>
@@ -873,8 +878,12 @@ __global__ void __launch_bounds__(128) gs_search_plain(GsDevIndex I, GsBatch B)
                     rec.y = (int32_t)((uint32_t)(pos + 1) | 0x80000000u);
                 }
             }
-            uint64_t slot = fwd ? (uint64_t)(anchor - (k - 1)) : (uint64_t)n + (uint64_t)anchor;
-            slots[slot] = rec;
+            if (rec.y != 0) {
+                const uint64_t slot = B.slot_off[r] + (fwd ? (uint64_t)(anchor - (k - 1))
+                                                           : (uint64_t)n + (uint64_t)anchor);
+                slots[slot - B.slot_off[r]] = rec;
+                atomicOr(B.recmask + (slot >> 5), 1u << (slot & 31u));
+            }
         }
     }
     if (B.work) {

@@ -324,6 +324,30 @@ def test_graph_replay(small):
             assert_same(gres, ob, lens0.size, f"graph rep {rep}")
 
 
+def test_graph_replay_longer_reads(small):
+    """A pass captured on short reads, replayed on the same buffers holding
+    longer reads (more candidate slots than it was sized for): the replay
+    notices, sizes a new pass, and the seeds are the oracle's."""
+    import torch
+    dev = torch.device("cuda", 0)
+    short = sample_reads(small["codes"], 200, seed=97, lengths=(40,), err=0.01)
+    longr = sample_reads(small["codes"], 200, seed=98, lengths=(240,), err=0.01)
+    ctx = small["ctx"]
+    d_seqs = torch.zeros(200 * 240 + 16, dtype=torch.uint8, device=dev)
+    d_offs = torch.zeros(200, dtype=torch.int64, device=dev)
+    d_lens = torch.zeros(200, dtype=torch.int32, device=dev)
+    for reads in (short, short, longr, longr, short):
+        seqs, offs, lens = pack(reads)
+        d_seqs[:len(seqs)].copy_(torch.frombuffer(bytearray(seqs), dtype=torch.uint8))
+        d_offs.copy_(torch.from_numpy(offs.view(np.int64)))
+        d_lens.copy_(torch.from_numpy(lens.view(np.int32)))
+        torch.cuda.synchronize()
+        gres = ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), 200,
+                               fetch=True, k=19, smem=True, graph=True)
+        ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=True)
+        assert_same(gres, ob, 200, f"replay len {int(lens[0])}")
+
+
 def test_cli_record_input(small, tmp_path):
     """seed_gen -F reads multi-line FASTA, FASTQ, CR LF and gzip input; the
     records equal the oracle's on the joined sequences."""
