@@ -290,7 +290,12 @@ __global__ void gs_max_end_kernel(const uint64_t *off, const uint32_t *len, uint
                                   unsigned long long *out)
 {
     uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r < n) atomicMax(out, (unsigned long long)(off[r] + len[r]));
+    unsigned long long e = r < n ? (unsigned long long)(off[r] + len[r]) : 0ull;
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long t = __shfl_xor_sync(0xffffffffu, e, o);
+        e = t > e ? t : e;
+    }
+    if ((threadIdx.x & 31) == 0 && e) atomicMax(out, e);
 }
 
 template <class In, class Out>
@@ -680,21 +685,26 @@ extern "C" int gs_seed(gs_ctx *c, const char *seqs, const uint64_t *offsets,
     }
     RC(check_params(p));
     GS_CUDA(cudaSetDevice(gs_index_device(c->idx)));
-    uint64_t bytes = 0;
-    for (uint32_t r = 0; r < n_reads; r++) {
-        uint64_t e = offsets[r] + lengths[r];
-        if (e > bytes) bytes = e;
-    }
-    RC(grow(c->d_seqs, c->cap_seqs, bytes + 1));
+    /* offsets and lengths first; the end of the last base comes from a
+     * reduction on the device, then the bases themselves */
     RC(grow(c->d_offsets, c->cap_offsets, (size_t)n_reads + 1));
     RC(grow(c->d_lengths, c->cap_lengths, (size_t)n_reads + 1));
-    if (bytes) GS_CUDA(cudaMemcpyAsync(c->d_seqs, seqs, bytes, cudaMemcpyHostToDevice, c->st));
+    uint64_t bytes = 0;
     if (n_reads) {
         GS_CUDA(cudaMemcpyAsync(c->d_offsets, offsets, (size_t)n_reads * 8, cudaMemcpyHostToDevice,
                                 c->st));
         GS_CUDA(cudaMemcpyAsync(c->d_lengths, lengths, (size_t)n_reads * 4, cudaMemcpyHostToDevice,
                                 c->st));
+        GS_CUDA(cudaMemsetAsync(c->d_max, 0, 8, c->st));
+        gs_max_end_kernel<<<(n_reads + 255) / 256, 256, 0, c->st>>>(
+            c->d_offsets, c->d_lengths, n_reads, (unsigned long long *)c->d_max);
+        GS_CUDA(cudaGetLastError());
+        GS_CUDA(cudaMemcpyAsync(&c->h_small[12], c->d_max, 8, cudaMemcpyDeviceToHost, c->st));
+        GS_CUDA(cudaStreamSynchronize(c->st));
+        bytes = c->h_small[12];
     }
+    RC(grow(c->d_seqs, c->cap_seqs, bytes + 1));
+    if (bytes) GS_CUDA(cudaMemcpyAsync(c->d_seqs, seqs, bytes, cudaMemcpyHostToDevice, c->st));
     return run_pipeline(c, c->d_seqs, c->d_offsets, c->d_lengths, n_reads, p, 1);
 }
 

@@ -49,15 +49,15 @@ struct GsCont {
 };
 
 /* A candidate that survived its start in the batched search: its interval
- * I = [l,u] at far end pos and J = [jl,ju] (jl > ju: none), the interval of
- * the same string extended by one base toward the longer match (the
- * neighbour candidate's string at the same far end).  32 bytes. */
-struct __align__(32) GsWalker {
+ * I = [l,u] at the start's far end (anchor -/+ start length - 1) and
+ * J = [jl,ju] (jl > ju: none), the interval of the same string extended by
+ * one base toward the longer match (the neighbour candidate's string at the
+ * same far end) -- or, with the pending flag, the neighbour's own start
+ * interval, one base short of that far end.  24 bytes. */
+struct __align__(8) GsWalker {
     uint32_t r;
-    int32_t anchor;     /* bit 31: forward strand */
-    int32_t pos;
+    uint32_t anchor;    /* bits 0-29: anchor; bit 30: J pending; bit 31: forward strand */
     uint32_t l, u, jl, ju;
-    uint32_t pad;
 };
 
 /* Per-batch device arguments shared by the pipeline kernels. */

@@ -539,7 +539,8 @@ __global__ void __launch_bounds__(256, 5) gs_search_lockstep(GsDevIndex I, GsBat
  *     walker ends, from a per-warp window of the buffer. */
 
 #define GS_WALKER_HOLE 0xffffffffu
-#define GS_WALKER_JPEND 1u        /* pad flag: J is one base short of I's far end */
+#define GS_WALKER_JPEND 0x40000000u   /* anchor flag: J is one base short of I's far end */
+#define GS_WALKER_FWD 0x80000000u
 #define GS_WALKER_CHUNK 512u      /* buffer entries a warp reserves at a time */
 #define GS_WALK_WINDOW 256u       /* buffer entries a walk-pass warp takes at a time */
 
@@ -683,16 +684,16 @@ __device__ __forceinline__ void gs_start_item(const GsDevIndex &I, const GsBatch
         if (rank < rem) idx = res.next + rank;
         else idx = (uint64_t)g + (rank - rem);
         const uint64_t cap_end = rank < rem ? res.end : min((uint64_t)g + GS_WALKER_CHUNK, B.walker_cap);
-        if (idx < cap_end) {
+        /* the entry keeps 30 bits of anchor: reads of 2^30 bases or more
+         * (none in practice) are walked here */
+        if (idx < cap_end && iL < (1 << 30)) {
             GsWalker w;
             w.r = r;
-            w.anchor = (int32_t)((uint32_t)anchor | (fwd ? 0x80000000u : 0u));
-            w.pos = pos;
+            w.anchor = (uint32_t)anchor | (fwd ? GS_WALKER_FWD : 0u) | (jpend ? GS_WALKER_JPEND : 0u);
             w.l = l;
             w.u = u;
             w.jl = jl;
             w.ju = ju;
-            w.pad = jpend ? GS_WALKER_JPEND : 0u;
             B.walkers[idx] = w;
         } else {
             gs_walk_in_place<NSTOP, COUNT>(I, B, r, n, fwd, anchor, pos, l, u, jl, ju, jpend, wb);
@@ -770,9 +771,10 @@ __global__ void __launch_bounds__(128) gs_search_walk(GsDevIndex I, GsBatch B)
                 GsWalker w = B.walkers[win + rank];
                 if (w.r != GS_WALKER_HOLE) {
                     r = w.r;
-                    fwd = (w.anchor >> 31) != 0;
-                    anchor = w.anchor & 0x7fffffff;
-                    pos = w.pos;
+                    fwd = (w.anchor & GS_WALKER_FWD) != 0;
+                    anchor = (int)(w.anchor & (GS_WALKER_JPEND - 1u));
+                    dir = fwd ? -1 : 1;
+                    pos = anchor + dir * (gs_start_len(I, B.k) - 1);
                     l = w.l;
                     u = w.u;
                     jl = w.jl;
@@ -784,7 +786,7 @@ __global__ void __launch_bounds__(128) gs_search_walk(GsDevIndex I, GsBatch B)
                     seq = (const unsigned char *)B.seqs + B.offsets[r];
                     have = true;
                     killed = false;
-                    jpend = (w.pad & GS_WALKER_JPEND) != 0;
+                    jpend = (w.anchor & GS_WALKER_JPEND) != 0;
                 }
             }
             win += take;

@@ -54,12 +54,13 @@ struct Req {
 };
 
 /* device bytes one pass needs per base and per read: slots (2 x 16 B per
- * start position), the batched search's walker buffer (16 entries of 32 B
- * per work item of 31 start positions, about 33 B per base and 1 KB per
- * read), per-read counters, outputs (a few seeds and positions per read) */
+ * start position) and their record bitmap, the batched search's walker
+ * buffer (16 entries of 24 B per work item of 31 start positions, about
+ * 25 B per base and 0.8 KB per read), per-read counters, outputs (a few seeds
+ * and positions per read) */
 inline uint64_t estimate_bytes(uint64_t bases, uint64_t reads)
 {
-    return bases * 73 + reads * 1280 + (4u << 20);
+    return bases * 64 + reads * 1024 + (4u << 20);
 }
 
 }  // namespace
