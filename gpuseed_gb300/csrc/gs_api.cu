@@ -112,6 +112,8 @@ struct gs_ctx {
     cudaStream_t st;
     bool own_stream;
     cudaEvent_t ev0, ev_s0, ev_s1, ev1;
+    cudaStream_t st_copy;       /* copies seeds out while positions are located */
+    cudaEvent_t ev_emit;
     /* inputs staged by gs_seed_rec */
     char *d_seqs; size_t cap_seqs;
     uint64_t *d_offsets; size_t cap_offsets;
@@ -184,6 +186,8 @@ extern "C" int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out)
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev_s0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev_s1);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st_copy, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_emit, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&c->queue, 16);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_max, 16);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_work, 32);
@@ -255,6 +259,11 @@ extern "C" void gs_ctx_free(gs_ctx *c)
     if (c->ev_s0) cudaEventDestroy(c->ev_s0);
     if (c->ev_s1) cudaEventDestroy(c->ev_s1);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->ev_emit) cudaEventDestroy(c->ev_emit);
+    if (c->st_copy) {
+        cudaStreamSynchronize(c->st_copy);
+        cudaStreamDestroy(c->st_copy);
+    }
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     if (c->own_stream && c->st) cudaStreamDestroy(c->st);
     free(c);
@@ -465,7 +474,26 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     B.pmap = c->pmap;
     B.seed_cap = n_seeds + 1;
     B.pos_cap = n_pos + 1;
+    if (fetch) {
+        RC(grow_host(c->h_seed_off, c->cap_h_so, nr1));
+        RC(grow_host(c->h_pos_off, c->cap_h_po, nr1));
+        RC(grow_host(c->h_seeds, c->cap_h_seeds, n_seeds + 1));
+        RC(grow_host(c->h_pos, c->cap_h_pos, n_pos + 1));
+    }
     RC(gs_launch_finalize_emit(I, B, st));
+    if (fetch) {
+        /* seeds and per-read offsets are final here: copy them out on the
+         * side stream while the positions are located */
+        GS_CUDA(cudaEventRecord(c->ev_emit, st));
+        GS_CUDA(cudaStreamWaitEvent(c->st_copy, c->ev_emit, 0));
+        GS_CUDA(cudaMemcpyAsync(c->h_seed_off, c->seed_off, nr1 * 8, cudaMemcpyDeviceToHost,
+                                c->st_copy));
+        GS_CUDA(cudaMemcpyAsync(c->h_pos_off, c->pos_off, nr1 * 8, cudaMemcpyDeviceToHost,
+                                c->st_copy));
+        if (n_seeds)
+            GS_CUDA(cudaMemcpyAsync(c->h_seeds, c->seeds, n_seeds * sizeof(gs_seed_rec),
+                                    cudaMemcpyDeviceToHost, c->st_copy));
+    }
     RC(gs_launch_locate(I, B, n_seeds, n_pos, st));
     GS_CUDA(cudaEventRecord(c->ev1, st));
     GS_CUDA(cudaMemcpyAsync(&c->h_small[5], c->queue + 1, 4, cudaMemcpyDeviceToHost, st));
@@ -473,20 +501,10 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     if (B.work) GS_CUDA(cudaMemcpyAsync(&c->h_small[6], c->d_work, 32, cudaMemcpyDeviceToHost, st));
     c->n_seeds = n_seeds;
     c->n_pos = n_pos;
-    if (fetch) {
-        RC(grow_host(c->h_seed_off, c->cap_h_so, nr1));
-        RC(grow_host(c->h_pos_off, c->cap_h_po, nr1));
-        RC(grow_host(c->h_seeds, c->cap_h_seeds, n_seeds + 1));
-        RC(grow_host(c->h_pos, c->cap_h_pos, n_pos + 1));
-        GS_CUDA(cudaMemcpyAsync(c->h_seed_off, c->seed_off, nr1 * 8, cudaMemcpyDeviceToHost, st));
-        GS_CUDA(cudaMemcpyAsync(c->h_pos_off, c->pos_off, nr1 * 8, cudaMemcpyDeviceToHost, st));
-        if (n_seeds)
-            GS_CUDA(cudaMemcpyAsync(c->h_seeds, c->seeds, n_seeds * sizeof(gs_seed_rec),
-                                    cudaMemcpyDeviceToHost, st));
-        if (n_pos)
-            GS_CUDA(cudaMemcpyAsync(c->h_pos, c->pos, n_pos * 4, cudaMemcpyDeviceToHost, st));
-    }
+    if (fetch && n_pos)
+        GS_CUDA(cudaMemcpyAsync(c->h_pos, c->pos, n_pos * 4, cudaMemcpyDeviceToHost, st));
     GS_CUDA(cudaStreamSynchronize(st));
+    if (fetch) GS_CUDA(cudaStreamSynchronize(c->st_copy));
     uint32_t flags = (uint32_t)(c->h_small[5] & 0xffffffffu);
     c->last_walkers = c->last_walker_cap ? (c->h_small[10] & 0xffffffffu) : 0;
     if (!p->walker_slots && c->last_walker_cap && c->last_walkers >= c->last_walker_cap &&

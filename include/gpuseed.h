@@ -187,10 +187,12 @@ int gs_ctx_last_work(gs_ctx *ctx, uint64_t out[4]);
 int gs_ctx_last_walkers(gs_ctx *ctx, uint64_t *n_walkers, uint64_t *capacity);
 
 /* ---- autotuner ----------------------------------------------------------
- * Times the batched search on the first `sample` reads (device buffers) over
- * queue_chunk, handoff_lanes, handoff_steps and ctas_per_sm (coordinate
- * descent, two rounds) and writes the fastest setting into *p; *best_ms gets
- * its search time.  Results never depend on these knobs. */
+ * Times the search on the first `sample` reads (device buffers) by coordinate
+ * descent (two rounds) over the kernel's launch knobs -- queue_chunk and
+ * ctas_per_sm for GS_KERNEL_BATCHED, those and handoff_lanes/handoff_steps
+ * for GS_KERNEL_LOCKSTEP -- and writes the fastest setting into *p; *best_ms
+ * gets its search time.  Results never depend on these knobs.  No
+ * counterpart in the reference. */
 int gs_autotune(gs_ctx *ctx, const char *d_seqs, const uint64_t *d_offsets,
                 const uint32_t *d_lengths, uint32_t n_reads, gs_params *p, uint32_t sample,
                 float *best_ms);
