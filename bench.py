@@ -83,9 +83,11 @@ def workload(cfg, ref_len, n_reads, rank=0, load_gpu_index=True):
             idx = gs.Index(prefix)
         log(f"[bench] index files from cache, loaded in {time.time() - t0:.1f}s")
     else:
-        idx = gs.build_index(codes, 7, prefix=prefix + ".tmp", load=load_gpu_index)
+        # each rank writes its own files; the rename publishes them whole
+        tmp = f"{prefix}.tmp{rank}.{os.getpid()}"
+        idx = gs.build_index(codes, 7, prefix=tmp, load=load_gpu_index)
         for ext in (".bwt", ".sa"):
-            os.replace(prefix + ".tmp" + ext, prefix + ext)
+            os.replace(tmp + ext, prefix + ext)
         log(f"[bench] index built on GPU in {time.time() - t0:.1f}s")
     t0 = time.time()
     seqs, offs, lens = W.make_reads(codes, nmask, rspec)
