@@ -34,9 +34,10 @@ extern "C" {
 #define GS_ETIMEOUT -8   /* a bounded wait ran out */
 #define GS_ESTATE -9     /* call not valid in the object's current state */
 
-/* Semantics switches (defaults first).  See the design doc for the reference
- * behaviour each one reproduces. */
-#define GS_N_WILDCARD 0  /* non-ACGT base after the 13-mer: interval unchanged */
+/* Semantics switches (defaults first: the reference's behaviour). */
+#define GS_N_WILDCARD 0  /* non-ACGT base after the 13-mer: interval unchanged, as the
+                            reference's unassigned `base` test and find_occ_gpu's early
+                            return make it (seed_gen.cu:2125, :2246, :333) */
 #define GS_N_STOP 1      /* non-ACGT base stops the extension (bwa) */
 #define GS_LF_GPUSEED 0  /* LF(primary+1) = 0 as seed_gen.cu:455-458 */
 #define GS_LF_BWA 1      /* LF as bwa */

@@ -165,7 +165,7 @@ def test_cli_matches_oracle(small, tmp_path):
 
 
 def test_config1_full(built, tmp_path_factory):
-    """BASELINE config 1 at full size: 1 Mbp, 10,000 x 100 bp, k=20, MEM."""
+    """Config 1 at full size: 1 Mbp, 10,000 x 100 bp, k=20, MEM."""
     gs = _gs()
     from gpuseed_gb300 import workloads as W
     d = tmp_path_factory.mktemp("cfg1")
