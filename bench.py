@@ -217,7 +217,8 @@ def cpu_baseline(prefix, seqs, offs, lens, k, smem, table, target_s=12.0, thread
 # --------------------------------------------------------------------------
 # serving: Poisson arrivals of config-5 requests against the resident index
 
-def serving_sweep(idx, codes, nmask, k, smem, peak_reads_s, loads=(0.1, 0.5, 0.9, 1.2),
+def serving_sweep(idx, codes, nmask, k, smem, peak_reads_s, max_batch_reads=1 << 20, n_slots=4,
+                  loads=(0.1, 0.5, 0.9, 1.2), modes=("continuous", "per_request"),
                   seconds=1.5, seed=0x5EED1005):
     import gpuseed_gb300 as gs
     from gpuseed_gb300 import workloads as W
@@ -244,7 +245,7 @@ def serving_sweep(idx, codes, nmask, k, smem, peak_reads_s, loads=(0.1, 0.5, 0.9
     log(f"[bench] serving peak: batched pass over {plens.size:,} request reads at "
         f"{peak_reads_s:,.0f} reads/s")
     out = []
-    for mode in ("continuous", "per_request"):
+    for mode in modes:
         for load in loads:
             rate = load * peak_reads_s / mean_reads          # requests per second
             n_req = max(20, int(rate * seconds))
@@ -256,22 +257,35 @@ def serving_sweep(idx, codes, nmask, k, smem, peak_reads_s, loads=(0.1, 0.5, 0.9
             gaps = rng.exponential(1.0 / rate, n_req)
             starts = rng.integers(0, plens.size - 4096, n_req)
             if mode == "continuous":
-                srv = gs.Server(idx, n_slots=4, max_batch_reads=1 << 18, k=k, smem=smem)
+                srv = gs.Server(idx, n_slots=n_slots, max_batch_reads=max_batch_reads, k=k, smem=smem)
             else:
                 srv = gs.Server(idx, n_slots=1, max_batch_reads=1, k=k, smem=smem)
+            # warm-up: the same arrival process for a third of the time, so that
+            # the slots' workspaces reach their working size as in a running
+            # server; then the measured stream (stats as differences)
+            nw = max(10, n_req // 3)
+            srv.replay(pseqs, poffs, plens, starts[:nw], sizes[:nw], gaps[:nw] * 1e3)
+            st0 = srv.stats()
             lat, wall_ms, sub_ms = srv.replay(pseqs, poffs, plens, starts, sizes, gaps * 1e3)
-            st = srv.stats()
+            st1 = srv.stats()
             srv.stop()
+            st = {n: st1[n] - st0[n] for n in ("passes", "submit_us", "merge_us", "seed_us",
+                                                 "split_us")}
             out.append({"mode": mode, "load": load, "requests": n_req,
+                        "max_batch_reads": max_batch_reads if mode == "continuous" else 1,
                         "peak_reads_s": float(peak_reads_s),
                         "offered_reads_s": float(sizes.sum() / gaps.sum()),
                         "submitted_reads_s": float(sizes.sum() / (sub_ms / 1e3)),
                         "achieved_reads_s": float(sizes.sum() / (wall_ms / 1e3)),
                         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                        "passes": int(st["passes"])})
+                        "passes": int(st["passes"]),
+                        "host_ms": {n: st[n + "_us"] / 1e3 for n in ("submit", "merge", "seed", "split")}})
             log(f"[bench] serving {mode} load {load:.0%}: p50 {out[-1]['p50_ms']:.1f} ms "
-                f"p99 {out[-1]['p99_ms']:.1f} ms, {out[-1]['achieved_reads_s']:,.0f} reads/s, "
-                f"{st['passes']} passes for {n_req} requests")
+                f"p99 {out[-1]['p99_ms']:.1f} ms, {out[-1]['achieved_reads_s']:,.0f} reads/s "
+                f"(submitted {out[-1]['submitted_reads_s']:,.0f}), {st['passes']} passes for "
+                f"{n_req} requests; submit/merge/seed/split "
+                + "/".join(f"{st[n + '_us'] / 1e3:.0f}" for n in ("submit", "merge", "seed", "split"))
+                + " ms")
     return out
 
 
@@ -351,6 +365,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-text", action="store_true")
+    ap.add_argument("--serve-batch", type=int, default=1 << 20,
+                    help="serving: most reads merged into one pass")
     ap.add_argument("--retune", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -564,7 +580,8 @@ def main():
 
     latency = None
     if rank == 0 and not args.no_serving:
-        latency = serving_sweep(idx, w["codes"], w["nmask"], k, smem, value / ws)
+        latency = serving_sweep(idx, w["codes"], w["nmask"], k, smem, value / ws,
+                                max_batch_reads=args.serve_batch)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

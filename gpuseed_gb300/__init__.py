@@ -71,7 +71,8 @@ class ServerOpts(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("submitted", "completed", "failed", "passes", "reads",
                                           "max_batch_reads", "pending", "reserved_bytes",
-                                          "budget_bytes")]
+                                          "budget_bytes", "submit_us", "merge_us", "seed_us",
+                                          "split_us")]
 
 
 class IndexInfo(C.Structure):

@@ -79,15 +79,19 @@ size_t gs_index_occ_bytes(const gs_index *idx);
 /* ------------------------------------------------------------------ */
 /* context */
 
+/* Workspace growth is stream-ordered (the device's default memory pool):
+ * cudaFree would wait for the whole device, stalling every other context's
+ * work -- the serving loop's slots grow their workspaces while the others
+ * run. */
 template <class T>
-static int grow(T *&p, size_t &cap, size_t n)
+static int grow(T *&p, size_t &cap, size_t n, cudaStream_t st)
 {
     if (n <= cap && p) return GS_OK;
     size_t nc = n + n / 4 + 64;
     T *np = NULL;
-    cudaError_t e = cudaMalloc(&np, nc * sizeof(T));
-    if (e != cudaSuccess) return gs_cuda_fail(e, "cudaMalloc(workspace)");
-    cudaFree(p);
+    cudaError_t e = cudaMallocAsync((void **)&np, nc * sizeof(T), st);
+    if (e != cudaSuccess) return gs_cuda_fail(e, "cudaMallocAsync(workspace)");
+    if (p) cudaFreeAsync(p, st);
     p = np;
     cap = nc;
     return GS_OK;
@@ -313,10 +317,10 @@ static int exclusive_scan(gs_ctx *c, In in, Out out, size_t n)
     size_t bytes = 0;
     GS_CUDA(cub::DeviceScan::ExclusiveSum(NULL, bytes, in, out, (int64_t)n, c->st));
     if (bytes > c->cap_cub) {
-        cudaFree(c->cub_tmp);
+        if (c->cub_tmp) cudaFreeAsync(c->cub_tmp, c->st);
         c->cub_tmp = NULL;
         c->cap_cub = 0;
-        GS_CUDA(cudaMalloc(&c->cub_tmp, bytes));
+        GS_CUDA(cudaMallocAsync(&c->cub_tmp, bytes, c->st));
         c->cap_cub = bytes;
     }
     GS_CUDA(cub::DeviceScan::ExclusiveSum(c->cub_tmp, bytes, in, out, (int64_t)n, c->st));
@@ -360,16 +364,16 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     c->have_host = c->have_dev = 0;
     c->n_reads = n_reads;
     size_t nr1 = (size_t)n_reads + 1;
-    RC(grow(c->slot_cnt, c->cap_slot_cnt, nr1));
-    RC(grow(c->slot_off, c->cap_slot_off, nr1));
-    RC(grow(c->item_cnt, c->cap_item_cnt, nr1));
-    RC(grow(c->item_off, c->cap_item_off, nr1));
-    RC(grow(c->rd_nf, c->cap_nf, nr1));
-    RC(grow(c->rd_nr, c->cap_nr, nr1));
-    RC(grow(c->rd_nseeds, c->cap_rns, nr1));
-    RC(grow(c->rd_npos, c->cap_rnp, nr1));
-    RC(grow(c->seed_off, c->cap_so, nr1));
-    RC(grow(c->pos_off, c->cap_po, nr1));
+    RC(grow(c->slot_cnt, c->cap_slot_cnt, nr1, c->st));
+    RC(grow(c->slot_off, c->cap_slot_off, nr1, c->st));
+    RC(grow(c->item_cnt, c->cap_item_cnt, nr1, c->st));
+    RC(grow(c->item_off, c->cap_item_off, nr1, c->st));
+    RC(grow(c->rd_nf, c->cap_nf, nr1, c->st));
+    RC(grow(c->rd_nr, c->cap_nr, nr1, c->st));
+    RC(grow(c->rd_nseeds, c->cap_rns, nr1, c->st));
+    RC(grow(c->rd_npos, c->cap_rnp, nr1, c->st));
+    RC(grow(c->seed_off, c->cap_so, nr1, c->st));
+    RC(grow(c->pos_off, c->cap_po, nr1, c->st));
 
     GsBatch B;
     memset(&B, 0, sizeof(B));
@@ -408,21 +412,21 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     GS_CUDA(cudaStreamSynchronize(st));
     uint64_t n_slots = c->h_small[0];
     uint32_t n_items = (uint32_t)(c->h_small[1] & 0xffffffffu);
-    RC(grow(c->slots, c->cap_slots, n_slots + 1));
-    RC(grow(c->recmask, c->cap_recmask, (c->cap_slots + 31) / 32 + 1));
+    RC(grow(c->slots, c->cap_slots, n_slots + 1, c->st));
+    RC(grow(c->recmask, c->cap_recmask, (c->cap_slots + 31) / 32 + 1, c->st));
     B.slots = c->slots;
     B.slot_cap = c->cap_slots;
     B.recmask = c->recmask;
     GS_CUDA(cudaMemsetAsync(c->recmask, 0, ((n_slots + 31) / 32 + 1) * sizeof(uint32_t), st));
     B.item_cap = n_items;
     if (p->kernel == GS_KERNEL_PLAIN) {
-        RC(grow(c->hist, c->cap_hist, c->h_small[2] + 1));
+        RC(grow(c->hist, c->cap_hist, c->h_small[2] + 1, c->st));
         B.hist = c->hist;
     } else if (p->kernel == GS_KERNEL_LOCKSTEP && p->handoff_lanes >= 0) {
         B.handoff_lanes = p->handoff_lanes ? p->handoff_lanes : GS_HANDOFF_LANES;
         B.handoff_steps = p->handoff_steps > 0 ? p->handoff_steps : GS_HANDOFF_STEPS;
         if (B.handoff_lanes > 32) B.handoff_lanes = 32;
-        RC(grow(c->cont, c->cap_cont, (size_t)n_items * (size_t)B.handoff_lanes + 1));
+        RC(grow(c->cont, c->cap_cont, (size_t)n_items * (size_t)B.handoff_lanes + 1, c->st));
         B.cont = c->cont;
         B.cont_cap = c->cap_cont;
     }
@@ -435,7 +439,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
         const uint64_t per16 = p->walker_slots ? (uint64_t)p->walker_slots : c->walker_per16;
         uint64_t want = ((uint64_t)n_items * per16 + 15u) / 16u + 32u;
         if (want > (1ull << 31)) want = 1ull << 31;   /* 32-bit buffer counter */
-        RC(grow(c->walkers, c->cap_walkers, (size_t)want));
+        RC(grow(c->walkers, c->cap_walkers, (size_t)want, c->st));
         B.walkers = c->walkers;
         B.walker_cap = want;
         c->last_walker_cap = want;
@@ -462,10 +466,10 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
         gs_set_error("batch emits %llu positions; split the batch", (unsigned long long)n_pos);
         return GS_EOVERFLOW;
     }
-    RC(grow(c->seeds, c->cap_seeds, n_seeds + 1));
-    RC(grow(c->seed_pos, c->cap_seed_pos, n_seeds + 1));
-    RC(grow(c->pos, c->cap_pos, n_pos + 1));
-    RC(grow(c->pmap, c->cap_pmap, n_pos + 1));
+    RC(grow(c->seeds, c->cap_seeds, n_seeds + 1, c->st));
+    RC(grow(c->seed_pos, c->cap_seed_pos, n_seeds + 1, c->st));
+    RC(grow(c->pos, c->cap_pos, n_pos + 1, c->st));
+    RC(grow(c->pmap, c->cap_pmap, n_pos + 1, c->st));
     B.seed_off = c->seed_off;
     B.pos_off = c->pos_off;
     B.seeds = c->seeds;
@@ -705,8 +709,8 @@ extern "C" int gs_seed(gs_ctx *c, const char *seqs, const uint64_t *offsets,
     GS_CUDA(cudaSetDevice(gs_index_device(c->idx)));
     /* offsets and lengths first; the end of the last base comes from a
      * reduction on the device, then the bases themselves */
-    RC(grow(c->d_offsets, c->cap_offsets, (size_t)n_reads + 1));
-    RC(grow(c->d_lengths, c->cap_lengths, (size_t)n_reads + 1));
+    RC(grow(c->d_offsets, c->cap_offsets, (size_t)n_reads + 1, c->st));
+    RC(grow(c->d_lengths, c->cap_lengths, (size_t)n_reads + 1, c->st));
     uint64_t bytes = 0;
     if (n_reads) {
         GS_CUDA(cudaMemcpyAsync(c->d_offsets, offsets, (size_t)n_reads * 8, cudaMemcpyHostToDevice,
@@ -721,7 +725,7 @@ extern "C" int gs_seed(gs_ctx *c, const char *seqs, const uint64_t *offsets,
         GS_CUDA(cudaStreamSynchronize(c->st));
         bytes = c->h_small[12];
     }
-    RC(grow(c->d_seqs, c->cap_seqs, bytes + 1));
+    RC(grow(c->d_seqs, c->cap_seqs, bytes + 1, c->st));
     if (bytes) GS_CUDA(cudaMemcpyAsync(c->d_seqs, seqs, bytes, cudaMemcpyHostToDevice, c->st));
     return run_pipeline(c, c->d_seqs, c->d_offsets, c->d_lengths, n_reads, p, 1);
 }
@@ -862,8 +866,8 @@ static int format_text_device(gs_ctx *c, uint32_t first_read_no, int smem, uint6
     }
     cudaStream_t st = c->st;
     const uint64_t n_tok = 2ull * c->n_reads + c->n_seeds + c->n_pos;
-    RC(grow(c->t_sread, c->cap_t_sread, (size_t)c->n_seeds + 1));
-    RC(grow(c->t_off, c->cap_t_off, (size_t)n_tok + 1));
+    RC(grow(c->t_sread, c->cap_t_sread, (size_t)c->n_seeds + 1, c->st));
+    RC(grow(c->t_off, c->cap_t_off, (size_t)n_tok + 1, c->st));
     GsTextArgs a;
     memset(&a, 0, sizeof(a));
     a.n_reads = c->n_reads;
@@ -885,7 +889,7 @@ static int format_text_device(gs_ctx *c, uint32_t first_read_no, int smem, uint6
     GS_CUDA(cudaMemcpyAsync(&c->h_small[11], c->t_off + n_tok, 8, cudaMemcpyDeviceToHost, st));
     GS_CUDA(cudaStreamSynchronize(st));
     const uint64_t total = c->h_small[11];
-    RC(grow(c->t_text, c->cap_t_text, (size_t)total + 1));
+    RC(grow(c->t_text, c->cap_t_text, (size_t)total + 1, c->st));
     a.text = c->t_text;
     RC(gs_launch_text_write(a, st));
     *n_bytes = total;

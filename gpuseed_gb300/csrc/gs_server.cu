@@ -72,6 +72,10 @@ struct gs_server {
     std::condition_variable cv_work, cv_done;
     std::deque<Req *> pending;
     std::unordered_map<uint64_t, Req *> reqs;
+    /* released requests, kept with their buffers' capacity for the next
+     * submissions: copying into memory that was written before costs no page
+     * faults, which otherwise dominate copying requests in and seeds out */
+    std::vector<Req *> spare;
     std::vector<std::thread> workers;
     bool stopping;
     uint64_t next_id;
@@ -167,6 +171,7 @@ static void worker_main(gs_server *s, int slot)
         }
         double t0 = now_ms();
         uint64_t wb = 0, wr = 0;
+        double t_merged = 0, t_seeded = 0, t_split = 0;
         if (rc == GS_OK)
             for (Req *r : batch) {
                 r->t_start = t0;
@@ -178,7 +183,9 @@ static void worker_main(gs_server *s, int slot)
                 }
                 wb += r->bases;
             }
+        t_merged = now_ms();
         if (rc == GS_OK) rc = gs_seed(ctx, seqs, offs, lens, (uint32_t)nr, &s->opts.params);
+        t_seeded = now_ms();
         gs_result_view v;
         if (rc == GS_OK) rc = gs_result_host(ctx, &v);
         /* split */
@@ -199,14 +206,18 @@ static void worker_main(gs_server *s, int slot)
                 read0 += n;
             }
         }
+        t_split = now_ms();
         {
             std::lock_guard<std::mutex> lk(s->mu);
             double t1 = now_ms();
+            s->stats.merge_us += (uint64_t)((t_merged - t0) * 1e3);
+            s->stats.seed_us += (uint64_t)((t_seeded - t_merged) * 1e3);
+            s->stats.split_us += (uint64_t)((t_split - t_seeded) * 1e3);
             for (Req *r : batch) {
                 r->status = rc;
                 r->done = true;
                 r->t_done = t1;
-                std::vector<char>().swap(r->seqs);
+                r->seqs.clear();
                 if (rc == GS_OK) s->stats.completed++;
                 else s->stats.failed++;
             }
@@ -262,9 +273,22 @@ extern "C" int gs_server_submit(gs_server *s, const char *seqs, const uint64_t *
         gs_set_error("gs_server_submit: server params have k < 13");
         return GS_EINVAL;
     }
-    Req *r = new Req();
+    const double t_enter = now_ms();
+    Req *r = NULL;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (!s->spare.empty()) {
+            r = s->spare.back();
+            s->spare.pop_back();
+        }
+    }
+    if (!r) r = new Req();
     uint64_t bytes = 0;
     for (uint32_t i = 0; i < n_reads; i++) bytes += lengths[i];
+    r->seed_off.clear();
+    r->pos_off.clear();
+    r->seeds.clear();
+    r->pos.clear();
     r->seqs.resize(bytes);
     r->offs.resize(n_reads);
     r->lens.assign(lengths, lengths + n_reads);
@@ -281,6 +305,7 @@ extern "C" int gs_server_submit(gs_server *s, const char *seqs, const uint64_t *
     r->t_submit = now_ms();
     {
         std::lock_guard<std::mutex> lk(s->mu);
+        s->stats.submit_us += (uint64_t)((r->t_submit - t_enter) * 1e3);
         if (s->stopping) {
             delete r;
             gs_set_error("server is stopping");
@@ -344,8 +369,13 @@ extern "C" int gs_server_release(gs_server *s, uint64_t id)
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->reqs.find(id);
     if (it == s->reqs.end() || !it->second->done) return GS_ESTATE;
-    delete it->second;
+    Req *r = it->second;
     s->reqs.erase(it);
+    const size_t held = r->seqs.capacity() + r->offs.capacity() * 8 + r->lens.capacity() * 4 +
+                        r->seed_off.capacity() * 16 + r->seeds.capacity() * sizeof(gs_seed_rec) +
+                        r->pos.capacity() * 4;
+    if (s->spare.size() < 1024 && held <= ((size_t)32 << 20)) s->spare.push_back(r);
+    else delete r;
     return GS_OK;
 }
 
@@ -370,6 +400,7 @@ extern "C" void gs_server_stop(gs_server *s)
     s->cv_work.notify_all();
     for (auto &t : s->workers) t.join();
     for (auto &kv : s->reqs) delete kv.second;
+    for (Req *r : s->spare) delete r;
     delete s;
 }
 
@@ -387,11 +418,27 @@ extern "C" int gs_server_replay(gs_server *s, const char *pool_seqs, const uint6
         return GS_EINVAL;
     std::vector<uint64_t> ids(n_req);
     std::vector<uint64_t> offs;
+    int status = GS_OK;
+    uint32_t next_done = 0;
+    /* a client that takes each result as it is done (in submission order)
+     * and releases it, so the server reuses its buffers */
+    auto collect = [&](uint32_t upto, bool block) {
+        while (next_done < upto) {
+            int rc = gs_server_wait(s, ids[next_done], block ? -1 : 0);
+            if (rc == GS_ETIMEOUT) return;
+            gs_result_view v;
+            if (rc == GS_OK) rc = gs_server_result(s, ids[next_done], &v, &latency_ms[next_done]);
+            if (rc && !status) status = rc;
+            gs_server_release(s, ids[next_done]);
+            next_done++;
+        }
+    };
     double t0 = now_ms(), due = t0;
     for (uint32_t i = 0; i < n_req; i++) {
         due += gap_ms[i];
         double now;
         while ((now = now_ms()) < due) {
+            collect(i, false);
             if (due - now > 0.2) std::this_thread::sleep_for(std::chrono::microseconds(50));
         }
         const uint32_t f = first[i], n = count[i];
@@ -402,14 +449,7 @@ extern "C" int gs_server_replay(gs_server *s, const char *pool_seqs, const uint6
         if (rc) return rc;
     }
     double t_sub = now_ms();
-    int status = GS_OK;
-    for (uint32_t i = 0; i < n_req; i++) {
-        int rc = gs_server_wait(s, ids[i], -1);
-        gs_result_view v;
-        if (rc == GS_OK) rc = gs_server_result(s, ids[i], &v, &latency_ms[i]);
-        if (rc && !status) status = rc;
-        gs_server_release(s, ids[i]);
-    }
+    collect(n_req, true);
     if (wall_ms) *wall_ms = now_ms() - t0;
     if (submit_ms) *submit_ms = t_sub - t0;
     return status;

@@ -216,6 +216,10 @@ typedef struct {
 typedef struct {
     uint64_t submitted, completed, failed, passes, reads, max_batch_reads;
     uint64_t pending, reserved_bytes, budget_bytes;
+    /* cumulative microseconds: copying requests in (gs_server_submit), merging
+     * a pass's requests into pinned memory, the pass itself (gs_seed: copies
+     * and GPU), splitting its seeds back per request */
+    uint64_t submit_us, merge_us, seed_us, split_us;
 } gs_server_stats;
 int gs_server_start(gs_index *idx, const gs_server_opts *opts, gs_server **out);
 /* Copies the request's reads; the caller's buffers are free on return. */
