@@ -86,27 +86,57 @@ __device__ __forceinline__ void gs_rev_rule(const GsRec *Rv, uint32_t nr, uint32
     if (max_occ && sz > max_occ) keep = false;
 }
 
-/* compacts the records among slots s0..s0+n (flagged in the record mask;
+/* Compacts the records among slots s0..s0+n (flagged in the record mask;
  * the other slots were never written) to the front, in order; returns the
- * count.  Only flagged slots are read. */
+ * count.  Per 1024 slots: one round of mask words (a lane each, scanned
+ * across the warp), then the records, 32 at a time -- lane j finds the j-th
+ * set bit by binary lifting over the scan and __fns within its word.  A
+ * record's target is never beyond its source, and a group's loads all come
+ * before its writes, so compacting in place is safe. */
 __device__ __forceinline__ uint32_t gs_warp_compact(GsRec *slots, const uint32_t *mask, uint64_t s0,
                                                     uint32_t n, int lane)
 {
     uint32_t cnt = 0;
-    for (uint32_t c0 = 0; c0 < n; c0 += 32) {
-        const uint32_t i = c0 + (uint32_t)lane;
-        GsRec r;
-        bool v = false;
-        if (i < n) {
-            const uint64_t g = s0 + i;
-            v = (mask[g >> 5] >> (g & 31u)) & 1u;
-            if (v) r = slots[g];
+    if (n == 0) return 0;
+    const uint64_t s1 = s0 + n;
+    const uint64_t w0 = s0 >> 5, wend = (s1 + 31) >> 5;
+    for (uint64_t wc = w0; wc < wend; wc += 32) {
+        const uint64_t w = wc + (uint64_t)lane;
+        uint32_t m = 0;
+        if (w < wend) {
+            m = mask[w];
+            const uint64_t lo = w << 5;
+            if (lo < s0) m &= 0xffffffffu << (uint32_t)(s0 - lo);
+            if (lo + 32 > s1) m &= 0xffffffffu >> (uint32_t)(lo + 32 - s1);
         }
-        uint32_t m = __ballot_sync(0xffffffffu, v);
-        __syncwarp();
-        if (v) slots[s0 + cnt + __popc(m & ((1u << lane) - 1u))] = r;
-        __syncwarp();
-        cnt += __popc(m);
+        const uint32_t c = __popc(m);
+        uint32_t inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+        for (uint32_t g = 0; g < total; g += 32) {
+            const uint32_t j = g + (uint32_t)lane;
+            const uint32_t jj = j < total ? j : total - 1u;
+            int L = 0;   /* first lane whose inclusive count exceeds jj */
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                uint32_t x = __shfl_sync(0xffffffffu, inc, L + step - 1);
+                if (x <= jj) L += step;
+            }
+            const uint32_t word = __shfl_sync(0xffffffffu, m, L);
+            const uint32_t before = __shfl_sync(0xffffffffu, inc - c, L);
+            const uint32_t bit = __fns(word, 0, (int)(jj - before) + 1);
+            GsRec rec;
+            const bool v = j < total;
+            if (v) rec = slots[((wc + (uint64_t)L) << 5) + bit];
+            __syncwarp();
+            if (v) slots[s0 + cnt + j] = rec;
+            __syncwarp();
+        }
+        cnt += total;
     }
     return cnt;
 }
