@@ -412,7 +412,10 @@ def main():
                                   sample=min(n_reads, 1 << 20), k=k, smem=smem)
         cache[tag] = {"knobs": knobs, "sample_search_ms": tms}
         try:
-            json.dump(cache, open(tune_path, "w"), indent=1)
+            tmp = f"{tune_path}.{os.getpid()}"
+            with open(tmp, "w") as f:
+                json.dump(cache, f, indent=1)
+            os.replace(tmp, tune_path)
         except OSError:
             pass
         log(f"[bench] autotuned {knobs} ({tms:.1f} ms on the sample) in {time.time() - t0:.1f}s")
