@@ -738,7 +738,7 @@ __global__ void __launch_bounds__(256, 3) gs_search_start(GsDevIndex I, GsBatch 
 }
 
 template <int NSTOP, int COUNT>
-__global__ void __launch_bounds__(128) gs_search_walk(GsDevIndex I, GsBatch B)
+__global__ void __launch_bounds__(128, 8) gs_search_walk(GsDevIndex I, GsBatch B)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
