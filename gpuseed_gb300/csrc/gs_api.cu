@@ -18,6 +18,8 @@
 
 #include <cub/cub.cuh>
 
+#include <atomic>
+
 #include <errno.h>
 #include <stdarg.h>
 #include <stdlib.h>
@@ -205,13 +207,12 @@ extern "C" int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out)
      * a context of this process set it, it stays until reset.  On the
      * search's random accesses it costs time (70.9 -> 94.4 ms on 4M reads of
      * a 3.1 Gbp index), so a context made with the window off releases it. */
-    static bool persisting_set = false;
+    static std::atomic<bool> persisting_set(false);   /* contexts are made from many threads */
     float ratio = gs_index_l2_ratio(idx);
-    if (ratio <= 0.f && persisting_set) {
+    if (ratio <= 0.f && persisting_set.exchange(false)) {
         cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
         cudaCtxResetPersistingL2Cache();
         cudaGetLastError();
-        persisting_set = false;
     }
     if (ratio > 0.f) {
         int dev = gs_index_device(idx), maxwin = 0, persist = 0;
@@ -221,7 +222,7 @@ extern "C" int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out)
             size_t occ = gs_index_occ_bytes(idx);
             size_t win = occ < (size_t)maxwin ? occ : (size_t)maxwin;
             cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, (size_t)persist);
-            persisting_set = true;
+            persisting_set.store(true);
             cudaStreamAttrValue v;
             memset(&v, 0, sizeof(v));
             v.accessPolicyWindow.base_ptr = (void *)gs_index_dev(idx)->occ;
