@@ -119,3 +119,34 @@ def test_config3_full_size(built, tmp_path):
                 assert np.array_equal(codes[p:p + seg.size], seg), (r, x, y, p)
                 checked += 1
     assert checked > 200_000
+
+
+def test_very_long_reads(built, tmp_path):
+    """Reads of 50-100 kbp (one an exact 80 kbp copy, whose last candidate walks
+    80,000 steps) over a 400 kbp reference with a 20 kbp duplicated segment:
+    every kernel gives the oracle's seeds (its containment-stopped walk: the
+    unpruned one would take ~10^9 steps on the exact read)."""
+    import gpuseed_gb300 as gs
+    rng = np.random.default_rng(0x10C5)
+    codes = rng.integers(0, 4, 400_000, dtype=np.uint8)
+    codes[300_000:320_000] = codes[100_000:120_000]
+    prefix, idx = _gpu_index(tmp_path, codes, "long")
+    text = np.frombuffer(b"ACGT", np.uint8)[codes]
+    reads = []
+    for L in (50_000, 70_000, 100_000):
+        st = int(rng.integers(0, codes.size - L))
+        s = text[st:st + L].copy()
+        errs = rng.random(L) < 0.005
+        s[errs] = np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, int(errs.sum()))]
+        reads.append(s.tobytes())
+    reads.append(text[90_000:170_000].tobytes())          # exact, spans the duplicated segment
+    reads.append(b"ACGT" * 10 + text[5_000:60_000].tobytes())
+    lens = np.array([len(r) for r in reads], np.uint32)
+    offs = np.concatenate([[0], np.cumsum(lens[:-1])]).astype(np.uint64)
+    seqs = b"".join(reads)
+    ctx = gs.Context(idx)
+    oidx = pyoracle.Index(prefix)
+    for smem, k in ((True, 19), (False, 20)):
+        ob = oidx.seed(seqs, offs, lens, k=k, smem=smem, pruned=True)
+        for kernel in (0, 1, 2):
+            _compare(ctx.seed(seqs, offs, lens, k=k, smem=smem, kernel=kernel), ob, lens.size)
