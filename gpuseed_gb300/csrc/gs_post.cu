@@ -141,6 +141,72 @@ __device__ __forceinline__ uint32_t gs_warp_compact(GsRec *slots, const uint32_t
     return cnt;
 }
 
+/* Both strands of a read at once when their 2n slots fit one 1024-slot
+ * round: forward records (slots s0..s0+n) go to s0 + rank, reverse ones
+ * (s0+n..s0+2n) to s0 + n + rank -- one round of mask words, one of
+ * records, for both.  Every target is at or before its source and earlier
+ * records' targets lie before later records' sources, so in place is safe. */
+__device__ __forceinline__ void gs_warp_compact_both(GsRec *slots, const uint32_t *mask, uint64_t s0,
+                                                     uint32_t n, int lane, uint32_t &nf,
+                                                     uint32_t &nr)
+{
+    const uint64_t s1 = s0 + n, s2 = s0 + 2ull * n;
+    const uint64_t w0 = s0 >> 5, wend = (s2 + 31) >> 5;   /* at most 32 words */
+    const uint64_t w = w0 + (uint64_t)lane;
+    uint32_t mf = 0, mr = 0;
+    if (w < wend) {
+        uint32_t m = mask[w];
+        const uint64_t lo = w << 5;
+        if (lo < s0) m &= 0xffffffffu << (uint32_t)(s0 - lo);
+        if (lo + 32 > s2) m &= 0xffffffffu >> (uint32_t)(lo + 32 - s2);
+        /* bits below s1 are forward slots */
+        const uint32_t fmask = s1 <= lo ? 0u : (s1 >= lo + 32 ? 0xffffffffu
+                                                              : ~(0xffffffffu << (uint32_t)(s1 - lo)));
+        mf = m & fmask;
+        mr = m & ~fmask;
+    }
+    const uint32_t cf = __popc(mf), cr = __popc(mr);
+    uint32_t incf = cf, incr = cr;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t tf = __shfl_up_sync(0xffffffffu, incf, o);
+        uint32_t tr = __shfl_up_sync(0xffffffffu, incr, o);
+        if (lane >= o) {
+            incf += tf;
+            incr += tr;
+        }
+    }
+    nf = __shfl_sync(0xffffffffu, incf, 31);
+    nr = __shfl_sync(0xffffffffu, incr, 31);
+    const uint32_t total = nf + nr;
+    for (uint32_t g = 0; g < total; g += 32) {
+        const uint32_t j = g + (uint32_t)lane;
+        const bool v = j < total;
+        const bool rev = j >= nf;
+        const uint32_t jj = !v ? 0u : (rev ? j - nf : j);
+        int L = 0;   /* first lane whose inclusive count (of this strand) exceeds jj */
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const uint32_t xf = __shfl_sync(0xffffffffu, incf, L + step - 1);
+            const uint32_t xr = __shfl_sync(0xffffffffu, incr, L + step - 1);
+            if ((rev ? xr : xf) <= jj) L += step;
+        }
+        const uint32_t wf = __shfl_sync(0xffffffffu, mf, L);
+        const uint32_t wr = __shfl_sync(0xffffffffu, mr, L);
+        const uint32_t bf = __shfl_sync(0xffffffffu, incf - cf, L);
+        const uint32_t br = __shfl_sync(0xffffffffu, incr - cr, L);
+        GsRec rec;
+        if (v) {
+            const uint32_t word = rev ? wr : wf;
+            const uint32_t bit = __fns(word, 0, (int)(jj - (rev ? br : bf)) + 1);
+            rec = slots[((w0 + (uint64_t)L) << 5) + bit];
+        }
+        __syncwarp();
+        if (v) slots[(rev ? s1 : s0) + jj] = rec;
+        __syncwarp();
+    }
+}
+
 __global__ void __launch_bounds__(256) gs_finalize_count(GsBatch B)
 {
     const int lane = threadIdx.x & 31;
@@ -163,8 +229,13 @@ __global__ void __launch_bounds__(256) gs_finalize_count(GsBatch B)
         uint32_t n = (uint32_t)((B.slot_off[r + 1] - base) >> 1);
         GsRec *F = B.slots + base;
         GsRec *Rv = F + n;
-        uint32_t nf = gs_warp_compact(B.slots, B.recmask, base, n, lane);
-        uint32_t nr = gs_warp_compact(B.slots, B.recmask, base + n, n, lane);
+        uint32_t nf, nr;
+        if (2u * n + 31u <= 1024u) {
+            gs_warp_compact_both(B.slots, B.recmask, base, n, lane, nf, nr);
+        } else {
+            nf = gs_warp_compact(B.slots, B.recmask, base, n, lane);
+            nr = gs_warp_compact(B.slots, B.recmask, base + n, n, lane);
+        }
         uint64_t seeds = 0, npos = 0;
         for (uint32_t o = lane; o < nf; o += 32) {
             bool keep; uint32_t cnt, xl, xu;
