@@ -25,12 +25,12 @@ GS_ERRORS = {-1: "EINVAL", -2: "EIO", -3: "EFORMAT", -4: "ENOMEM", -5: "ECUDA", 
              -7: "EOVERFLOW", -8: "ETIMEOUT", -9: "ESTATE"}
 
 # Every symbol include/gpuseed.h declares.
-EXPORTS = ["gs_index_load", "gs_index_from_host", "gs_index_build", "gs_index_set_kmer_len", "gs_index_free", "gs_index_get_info",
+EXPORTS = ["gs_index_load", "gs_index_from_host", "gs_index_build", "gs_index_set_kmer_len", "gs_index_set_text", "gs_index_text_table", "gs_index_free", "gs_index_get_info",
            "gs_index_kmer_table", "gs_index_set_l2_window", "gs_ctx_create", "gs_ctx_free",
            "gs_seed", "gs_seed_device", "gs_result_host", "gs_result_device",
            "gs_result_write_text", "gs_result_write_text_host", "gs_result_text_device",
            "gs_ctx_stream", "gs_ctx_last_timing", "gs_ctx_last_work",
-           "gs_ctx_last_walkers",
+           "gs_ctx_last_walkers", "gs_ctx_last_text_jobs",
            "gs_seed_noalloc", "gs_autotune", "gs_server_start", "gs_server_submit", "gs_server_wait",
            "gs_server_result", "gs_server_release", "gs_server_get_stats", "gs_server_stop", "gs_server_replay",
            "gs_last_error",
@@ -78,7 +78,7 @@ class ServerStats(C.Structure):
 class IndexInfo(C.Structure):
     _fields_ = [("seq_len", C.c_uint32), ("primary", C.c_uint32), ("sa_intv", C.c_uint32),
                 ("n_sa", C.c_uint32), ("L2", C.c_uint32 * 5), ("device", C.c_int32),
-                ("device_bytes", C.c_uint64), ("kmer_len", C.c_int32)]
+                ("device_bytes", C.c_uint64), ("kmer_len", C.c_int32), ("text_min", C.c_int32)]
 
 
 _lib = None
@@ -101,6 +101,8 @@ def lib():
         L.gs_index_kmer_table.argtypes = [vp, u64, u64, vp]
         L.gs_index_set_l2_window.argtypes = [vp, C.c_float]
         L.gs_index_set_kmer_len.argtypes = [vp, i32]
+        L.gs_index_set_text.argtypes = [vp, i32]
+        L.gs_index_text_table.argtypes = [vp, i32, u64, u64, vp]
         L.gs_ctx_create.argtypes = [vp, vp, C.POINTER(vp)]
         L.gs_ctx_free.argtypes = [vp]
         L.gs_seed.argtypes = [vp, vp, vp, vp, u32, C.POINTER(Params)]
@@ -115,6 +117,7 @@ def lib():
         L.gs_ctx_last_timing.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         L.gs_ctx_last_work.argtypes = [vp, vp]
         L.gs_ctx_last_walkers.argtypes = [vp, C.POINTER(u64), C.POINTER(u64)]
+        L.gs_ctx_last_text_jobs.argtypes = [vp, C.POINTER(u64), C.POINTER(u64)]
         L.gs_autotune.argtypes = [vp, vp, vp, vp, u32, C.POINTER(Params), u32, C.POINTER(C.c_float)]
         L.gs_server_start.argtypes = [vp, C.POINTER(ServerOpts), C.POINTER(vp)]
         L.gs_server_submit.argtypes = [vp, vp, vp, vp, u32, C.POINTER(u64)]
@@ -181,6 +184,19 @@ class Index:
 
     def set_kmer_len(self, kmer_len: int):
         check(lib().gs_index_set_kmer_len(self.h, kmer_len))
+
+    def text_table(self, which: int) -> np.ndarray:
+        """Full SA (0), packed text words (1) or inverse-SA samples (2)."""
+        info = self.info()
+        n = {0: info.seq_len + 1, 1: (info.seq_len + 15) // 16, 2: info.seq_len // 4 + 1}[which]
+        out = np.empty(n, dtype=np.uint32)
+        check(lib().gs_index_text_table(self.h, which, 0, n, _ptr(out)))
+        return out
+
+    def set_text(self, min_steps: int):
+        """Text structures: > 0 build and enter text mode after min_steps
+        one-row steps; < 0 build, locate only; 0 free them."""
+        check(lib().gs_index_set_text(self.h, min_steps))
 
     def set_l2_window(self, hit_ratio: float):
         check(lib().gs_index_set_l2_window(self.h, hit_ratio))
@@ -332,6 +348,12 @@ class Context:
         """(walkers handed to the walk pass, buffer capacity) of the last batched pass."""
         n, cap = C.c_uint64(), C.c_uint64()
         check(lib().gs_ctx_last_walkers(self.h, C.byref(n), C.byref(cap)))
+        return int(n.value), int(cap.value)
+
+    def last_text_jobs(self):
+        """(walkers handed to the text pass, room for them) of the last batched pass."""
+        n, cap = C.c_uint64(), C.c_uint64()
+        check(lib().gs_ctx_last_text_jobs(self.h, C.byref(n), C.byref(cap)))
         return int(n.value), int(cap.value)
 
     def last_timing(self):

@@ -75,6 +75,7 @@ extern "C" int gs_version(void) { return 100; }
 
 const GsDevIndex *gs_index_dev(const gs_index *idx);
 int gs_index_device(const gs_index *idx);
+uint32_t gs_index_generation(const gs_index *idx);
 float gs_index_l2_ratio(const gs_index *idx);
 size_t gs_index_occ_bytes(const gs_index *idx);
 
@@ -140,6 +141,8 @@ struct gs_ctx {
     uint32_t *pmap; size_t cap_pmap;
     GsCont *cont; size_t cap_cont;
     GsWalker *walkers; size_t cap_walkers;
+    GsTextJob *text_jobs; size_t cap_text_jobs;
+    uint64_t last_text_cap, last_text_jobs;
     /* text formatting on the GPU */
     uint32_t *t_sread; size_t cap_t_sread;
     uint64_t *t_off; size_t cap_t_off;
@@ -169,6 +172,7 @@ struct gs_ctx {
     const uint64_t *g_offs;
     const uint32_t *g_lens;
     uint32_t g_n;
+    uint32_t g_gen;   /* index generation the graph was captured with */
     gs_params g_params;
     uint32_t g_items;
 };
@@ -194,7 +198,7 @@ extern "C" int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out)
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st_copy, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_emit, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaMalloc(&c->queue, 16);
+    if (e == cudaSuccess) e = cudaMalloc(&c->queue, 32);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_max, 16);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_work, 32);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_small, 256);
@@ -250,6 +254,7 @@ extern "C" void gs_ctx_free(gs_ctx *c)
     cudaFree(c->pos); cudaFree(c->pmap); cudaFree(c->queue); cudaFree(c->d_max);
     cudaFree(c->cont);
     cudaFree(c->walkers);
+    cudaFree(c->text_jobs);
     cudaFree(c->recmask);
     cudaFree(c->t_sread); cudaFree(c->t_off); cudaFree(c->t_text);
     cudaFreeHost(c->h_text[0]); cudaFreeHost(c->h_text[1]);
@@ -288,6 +293,14 @@ extern "C" int gs_ctx_last_walkers(gs_ctx *c, uint64_t *n_walkers, uint64_t *cap
     if (!c) return GS_EINVAL;
     if (n_walkers) *n_walkers = c->last_walkers;
     if (capacity) *capacity = c->last_walker_cap;
+    return GS_OK;
+}
+
+extern "C" int gs_ctx_last_text_jobs(gs_ctx *c, uint64_t *n_jobs, uint64_t *capacity)
+{
+    if (!c) return GS_EINVAL;
+    if (n_jobs) *n_jobs = c->last_text_jobs;
+    if (capacity) *capacity = c->last_text_cap;
     return GS_OK;
 }
 
@@ -393,7 +406,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
 
     GS_CUDA(cudaEventRecord(c->ev0, st));
     if (B.work) GS_CUDA(cudaMemsetAsync(c->d_work, 0, 32, st));
-    GS_CUDA(cudaMemsetAsync(c->queue, 0, 16, st));
+    GS_CUDA(cudaMemsetAsync(c->queue, 0, 32, st));
     B.slot_off = c->slot_cnt;
     B.item_off = c->item_cnt;
     RC(gs_launch_prepare(B, st));
@@ -432,6 +445,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
         B.cont_cap = c->cap_cont;
     }
     c->last_walker_cap = 0;
+    c->last_text_cap = 0;
     if (p->kernel == GS_KERNEL_BATCHED && p->walker_slots >= 0) {
         /* entries per 16 work items: as asked, or automatic -- 16 per item
          * with a start table (forced codes settle most candidates), all 31
@@ -444,6 +458,17 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
         B.walkers = c->walkers;
         B.walker_cap = want;
         c->last_walker_cap = want;
+        /* walkers handed to the text pass: two per work item is far above
+         * what reads with a few differences per 100 bases need; without
+         * room a walker walks on in the walk pass */
+        if (I.text_min) {
+            uint64_t tw = (uint64_t)n_items * 2u + 64u;
+            if (tw > (1ull << 31)) tw = 1ull << 31;
+            RC(grow(c->text_jobs, c->cap_text_jobs, (size_t)tw, c->st));
+            B.text_jobs = c->text_jobs;
+            B.text_cap = tw;
+            c->last_text_cap = tw;
+        }
     }
 
     GS_CUDA(cudaEventRecord(c->ev_s0, st));
@@ -503,6 +528,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     GS_CUDA(cudaEventRecord(c->ev1, st));
     GS_CUDA(cudaMemcpyAsync(&c->h_small[5], c->queue + 1, 4, cudaMemcpyDeviceToHost, st));
     GS_CUDA(cudaMemcpyAsync(&c->h_small[10], c->queue + 2, 4, cudaMemcpyDeviceToHost, st));
+    GS_CUDA(cudaMemcpyAsync(&c->h_small[11], c->queue + 4, 4, cudaMemcpyDeviceToHost, st));
     if (B.work) GS_CUDA(cudaMemcpyAsync(&c->h_small[6], c->d_work, 32, cudaMemcpyDeviceToHost, st));
     c->n_seeds = n_seeds;
     c->n_pos = n_pos;
@@ -512,6 +538,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     if (fetch) GS_CUDA(cudaStreamSynchronize(c->st_copy));
     uint32_t flags = (uint32_t)(c->h_small[5] & 0xffffffffu);
     c->last_walkers = c->last_walker_cap ? (c->h_small[10] & 0xffffffffu) : 0;
+    c->last_text_jobs = c->last_text_cap ? (c->h_small[11] & 0xffffffffu) : 0;
     if (!p->walker_slots && c->last_walker_cap && c->last_walkers >= c->last_walker_cap &&
         c->walker_per16 < 512u) {
         c->walker_per16 += c->walker_per16 / 2;
@@ -571,7 +598,7 @@ static int enqueue_pass(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     B.lf_mode = p->lf_mode;
     B.max_occ = p->max_occ > 0 ? (uint32_t)p->max_occ : 0u;
     B.queue = c->queue;
-    GS_CUDA(cudaMemsetAsync(c->queue, 0, 16, st));
+    GS_CUDA(cudaMemsetAsync(c->queue, 0, 32, st));
     B.slot_off = c->slot_cnt;
     B.item_off = c->item_cnt;
     RC(gs_launch_prepare(B, st));
@@ -589,6 +616,10 @@ static int enqueue_pass(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     if (c->last_walker_cap && c->walkers) {
         B.walkers = c->walkers;
         B.walker_cap = c->last_walker_cap;
+        if (c->last_text_cap && c->text_jobs && I.text_min) {
+            B.text_jobs = c->text_jobs;
+            B.text_cap = c->last_text_cap;
+        }
     }
     RC(gs_launch_search(I, B, GS_KERNEL_BATCHED, p->queue_chunk, p->ctas_per_sm, 0, st));
     B.rd_nf = c->rd_nf;
@@ -617,6 +648,7 @@ static bool same_graph(const gs_ctx *c, const char *s, const uint64_t *o, const 
                        uint32_t n, const gs_params *p)
 {
     return c->gexec && c->g_seqs == s && c->g_offs == o && c->g_lens == l && c->g_n == n &&
+           c->g_gen == gs_index_generation(c->idx) &&
            memcmp(&c->g_params, p, sizeof(gs_params)) == 0;
 }
 
@@ -680,6 +712,7 @@ static int run_graph(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets,
     c->g_offs = d_offsets;
     c->g_lens = d_lengths;
     c->g_n = n_reads;
+    c->g_gen = gs_index_generation(c->idx);
     c->g_params = *p;
     return GS_OK;
 }

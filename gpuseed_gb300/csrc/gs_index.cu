@@ -10,7 +10,7 @@
  * sa[0] = -1 sentinel (:2711) and the 13-mer table is built in HBM
  * (:2888-2895).
  */
-#include "gs_internal.h"
+#include "gs_fm.cuh"
 
 #include <stdlib.h>
 #include <string.h>
@@ -22,11 +22,147 @@ struct gs_index {
     uint32_t *d_sa;
     uint2 *d_kmer;
     uint2 *d_kmerx;
-    size_t occ_bytes, sa_bytes, kmer_bytes, kmerx_bytes;
+    uint32_t *d_saf, *d_text, *d_isa;
+    size_t occ_bytes, sa_bytes, kmer_bytes, kmerx_bytes, text_bytes;
     float l2_hit_ratio;
+    uint32_t gen;   /* bumped whenever device pointers change */
 };
 
 extern "C" int gs_index_set_kmer_len(gs_index *idx, int kx);
+extern "C" int gs_index_set_text(gs_index *idx, int min_steps);
+
+#define GS_TEXT_MIN_DEFAULT 4
+#define GS_SAF_UNSET 0xfffffffeu
+#define GS_CHAIN_MAX (1u << 20)   /* LF steps one chain may take */
+
+/* Every row lies on one chain of LF steps that starts at a sampled row: the
+ * chain of sampled row i0 (text position s0) visits the rows of positions
+ * s0-1, s0-2, ... and ends before the next sampled row or at the row of
+ * position 0 (row primary, whose BWT symbol is $).  One thread per chain;
+ * the chains together take seq_len+1 LF steps.  The row of position s has
+ * BWT base T[s-1], so the same pass writes the text.  A chain that ends
+ * at a sampled row checks that row's sample against its own position, so
+ * the samples and the BWT are checked against each other.  stat: rows
+ * visited, errors, and (steps << 32 | position) of the chain step that reaches row
+ * primary+1 when that row is not sampled. */
+__global__ void gs_text_chain_kernel(GsDevIndex I, uint32_t *saf, uint8_t *t8, uint32_t *isa,
+                                     unsigned long long *stat)
+{
+    unsigned long long visited = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < I.n_sa; j += stride) {
+        if (*(volatile unsigned long long *)&stat[1]) break;
+        uint32_t row = (uint32_t)(j * I.sa_intv);
+        uint32_t s = j == 0 ? I.seq_len : I.sa[j];
+        for (uint32_t t = 0;; t++) {
+            /* a consistent index ends every chain within seq_len+1 steps;
+             * an inconsistent one may cycle: bounded, and the other chains
+             * give up once one has failed */
+            if (t > I.seq_len || t >= GS_CHAIN_MAX || s > I.seq_len || row > I.seq_len ||
+                ((t & 4095u) == 4095u && *(volatile unsigned long long *)&stat[1])) {
+                atomicAdd(&stat[1], 1ull);
+                break;
+            }
+            saf[row] = s;
+            visited++;
+            if (s % GS_ISA_STEP == 0) isa[s / GS_ISA_STEP] = row;
+            if (row == I.primary || s == 0) {
+                if (row != I.primary || s != 0) atomicAdd(&stat[1], 1ull);
+                break;
+            }
+            const uint32_t ka = row - (row > I.primary ? 1u : 0u);
+            const GsBlk B = gs_load_block(I.occ, ka >> 6);
+            const uint32_t word = gs_sel4((ka >> 4) & 3u, B.w[4], B.w[5], B.w[6], B.w[7]);
+            const uint32_t c = (word >> ((~ka & 15u) << 1)) & 3u;
+            t8[s - 1] = (uint8_t)c;
+            row = gs_L2(I, c) + gs_occ_in_block(B, ka, c);
+            s--;
+            if (row % I.sa_intv == 0) {
+                /* the next chain's sample must continue this one */
+                if (row > I.seq_len || (row ? I.sa[row / I.sa_intv] : I.seq_len) != s)
+                    atomicAdd(&stat[1], 1ull);
+                break;
+            }
+            if (row == I.primary + 1u) stat[2] = ((unsigned long long)(t + 1) << 32) | s;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) visited += __shfl_xor_sync(0xffffffffu, visited, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&stat[0], visited);
+}
+
+/* 16 bases of t8 per text word, base i at bits 2*(i & 15) */
+__global__ void gs_text_pack_kernel(const uint8_t *t8, uint32_t seq_len, uint32_t *text,
+                                    uint64_t n_words)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n_words; w += stride) {
+        uint32_t v = 0;
+        const uint64_t b = w * 16;
+        for (uint32_t i = 0; i < 16; i++)
+            if (b + i < seq_len) v |= ((uint32_t)t8[b + i] & 3u) << (2 * i);
+        text[w] = v;
+    }
+}
+
+/* rows the chains did not reach (a consistent index leaves none) */
+__global__ void gs_text_unset_kernel(const uint32_t *saf, uint64_t n, unsigned long long *stat)
+{
+    unsigned long long cnt = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        cnt += saf[i] == GS_SAF_UNSET;
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&stat[1], cnt);
+}
+
+int gs_build_text(GsDevIndex &I, uint32_t *saf, uint32_t *text, uint32_t *isa, cudaStream_t st)
+{
+    const uint64_t n_rows = (uint64_t)I.seq_len + 1;
+    const uint64_t n_words = ((uint64_t)I.seq_len + 15) / 16;
+    uint8_t *t8 = NULL;
+    unsigned long long *stat = NULL;
+    cudaError_t e;
+    if ((e = cudaMalloc(&t8, I.seq_len ? I.seq_len : 1)) != cudaSuccess)
+        return gs_cuda_fail(e, "cudaMalloc(text build)");
+    if ((e = cudaMalloc(&stat, 4 * sizeof(unsigned long long))) != cudaSuccess) {
+        cudaFree(t8);
+        return gs_cuda_fail(e, "cudaMalloc(text build)");
+    }
+    int rc = GS_OK;
+    unsigned long long h[4] = {0, 0, 0, 0};
+    if ((e = cudaMemsetAsync(stat, 0, 4 * sizeof(unsigned long long), st)) != cudaSuccess ||
+        (e = cudaMemsetAsync(saf, 0xfe, n_rows * 4, st)) != cudaSuccess ||
+        (e = cudaMemsetAsync(text, 0, (n_words + 2) * 4, st)) != cudaSuccess ||
+        (e = cudaMemsetAsync(isa, 0, ((uint64_t)I.seq_len / GS_ISA_STEP + 1) * 4, st)) !=
+            cudaSuccess) {
+        rc = gs_cuda_fail(e, "text build");
+    } else {
+        GsDevIndex D = I;
+        const uint64_t chains = I.n_sa;
+        uint32_t grid = (uint32_t)((chains + 255) / 256);
+        if (grid > 152u * 64u) grid = 152u * 64u;
+        gs_text_chain_kernel<<<grid ? grid : 1, 256, 0, st>>>(D, saf, t8, isa, stat);
+        gs_text_pack_kernel<<<152 * 16, 256, 0, st>>>(t8, I.seq_len, text, n_words);
+        gs_text_unset_kernel<<<152 * 16, 256, 0, st>>>(saf, n_rows, stat);
+        if ((e = cudaGetLastError()) != cudaSuccess ||
+            (e = cudaMemcpyAsync(h, stat, sizeof(h), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            rc = gs_cuda_fail(e, "text build");
+    }
+    cudaFree(t8);
+    cudaFree(stat);
+    if (rc) return rc;
+    if (h[0] != n_rows || h[1] != 0) {
+        gs_set_error("index does not describe one text: %llu of %llu rows reached, %llu errors",
+                     h[0], (unsigned long long)n_rows, h[1]);
+        return GS_EFORMAT;
+    }
+    const uint32_t minus1 = 0xffffffffu;
+    GS_CUDA(cudaMemcpy(saf, &minus1, 4, cudaMemcpyHostToDevice));
+    I.quirk_lo = (uint32_t)(h[2] & 0xffffffffu);
+    I.quirk_n = (uint32_t)(h[2] >> 32);
+    return GS_OK;
+}
 
 /* Longer start table by reference length: one table entry per distinct
  * kx-mer the text can hold (4^kx around seq_len) */
@@ -122,9 +258,12 @@ static int upload(uint32_t primary, const uint32_t L2_1to4[4], const uint32_t *b
         gs_index_free(idx);
         return rc;
     }
-    /* the longer table is an accelerator: without room for it, run without */
+    /* the longer table and the text structures are accelerators: without
+     * room for them, run without */
     for (int kx = auto_kmer_len(seq_len); kx > GS_K0; kx--)
         if (gs_index_set_kmer_len(idx, kx) == GS_OK) break;
+    cudaGetLastError();
+    (void)gs_index_set_text(idx, GS_TEXT_MIN_DEFAULT);
     cudaGetLastError();
     *out = idx;
     return GS_OK;
@@ -226,6 +365,9 @@ extern "C" void gs_index_free(gs_index *idx)
     cudaFree(idx->d_sa);
     cudaFree(idx->d_kmer);
     cudaFree(idx->d_kmerx);
+    cudaFree(idx->d_saf);
+    cudaFree(idx->d_text);
+    cudaFree(idx->d_isa);
     free(idx);
 }
 
@@ -238,8 +380,90 @@ extern "C" int gs_index_get_info(const gs_index *idx, gs_index_info *out)
     out->n_sa = idx->dev.n_sa;
     for (int c = 0; c < 5; c++) out->L2[c] = idx->dev.L2[c];
     out->device = idx->device;
-    out->device_bytes = idx->occ_bytes + idx->sa_bytes + idx->kmer_bytes + idx->kmerx_bytes;
+    out->device_bytes =
+        idx->occ_bytes + idx->sa_bytes + idx->kmer_bytes + idx->kmerx_bytes + idx->text_bytes;
     out->kmer_len = idx->dev.kx ? idx->dev.kx : GS_K0;
+    out->text_min = idx->d_saf ? (idx->dev.text_min ? idx->dev.text_min : -1) : 0;
+    return GS_OK;
+}
+
+uint32_t gs_index_generation(const gs_index *idx) { return idx->gen; }
+
+extern "C" int gs_index_text_table(const gs_index *idx, int which, uint64_t first, uint64_t count,
+                                   uint32_t *out)
+{
+    if (!idx || !out || which < 0 || which > 2) return GS_EINVAL;
+    if (!idx->d_saf) {
+        gs_set_error("the index has no text structures");
+        return GS_ESTATE;
+    }
+    const uint64_t n = which == 0   ? (uint64_t)idx->dev.seq_len + 1
+                       : which == 1 ? ((uint64_t)idx->dev.seq_len + 15) / 16
+                                    : (uint64_t)idx->dev.seq_len / GS_ISA_STEP + 1;
+    if (first > n || count > n - first) {
+        gs_set_error("text table range [%llu, +%llu) outside [0, %llu)", (unsigned long long)first,
+                     (unsigned long long)count, (unsigned long long)n);
+        return GS_EINVAL;
+    }
+    const uint32_t *src = which == 0 ? idx->d_saf : which == 1 ? idx->d_text : idx->d_isa;
+    GS_CUDA(cudaSetDevice(idx->device));
+    GS_CUDA(cudaMemcpy(out, src + first, count * 4, cudaMemcpyDeviceToHost));
+    return GS_OK;
+}
+
+static void drop_text(gs_index *idx)
+{
+    cudaFree(idx->d_saf);
+    cudaFree(idx->d_text);
+    cudaFree(idx->d_isa);
+    idx->d_saf = idx->d_text = idx->d_isa = NULL;
+    idx->text_bytes = 0;
+    GsDevIndex &D = idx->dev;
+    D.saf = D.text = D.isa = NULL;
+    D.quirk_lo = D.quirk_n = 0;
+    D.text_min = 0;
+}
+
+extern "C" int gs_index_set_text(gs_index *idx, int min_steps)
+{
+    if (!idx) return GS_EINVAL;
+    GS_CUDA(cudaSetDevice(idx->device));
+    GS_CUDA(cudaDeviceSynchronize());
+    idx->gen++;
+    if (min_steps == 0) {
+        drop_text(idx);
+        return GS_OK;
+    }
+    GsDevIndex &D = idx->dev;
+    if (!idx->d_saf) {
+        if (D.seq_len >= GS_REGIME_MARK) {
+            gs_set_error("text structures need seq_len below %u", GS_REGIME_MARK);
+            return GS_EINVAL;
+        }
+        const size_t saf_b = ((size_t)D.seq_len + 1) * 4;
+        const size_t text_b = (((size_t)D.seq_len + 15) / 16 + 2) * 4;
+        const size_t isa_b = ((size_t)D.seq_len / GS_ISA_STEP + 1) * 4;
+        cudaError_t e;
+        if ((e = cudaMalloc(&idx->d_saf, saf_b)) != cudaSuccess ||
+            (e = cudaMalloc(&idx->d_text, text_b)) != cudaSuccess ||
+            (e = cudaMalloc(&idx->d_isa, isa_b)) != cudaSuccess) {
+            drop_text(idx);
+            return gs_cuda_fail(e, "cudaMalloc(text structures)");
+        }
+        GsDevIndex B = D;
+        int rc = gs_build_text(B, idx->d_saf, idx->d_text, idx->d_isa, 0);
+        if (rc) {
+            drop_text(idx);
+            return rc;
+        }
+        idx->text_bytes = saf_b + text_b + isa_b;
+        D.saf = idx->d_saf;
+        D.text = idx->d_text;
+        D.isa = idx->d_isa;
+        D.quirk_lo = B.quirk_lo;
+        D.quirk_n = B.quirk_n;
+    }
+    D.text_min = min_steps > 0 ? min_steps : 0;
     return GS_OK;
 }
 
@@ -272,6 +496,8 @@ extern "C" int gs_index_set_kmer_len(gs_index *idx, int kx)
         return GS_EINVAL;
     }
     GS_CUDA(cudaSetDevice(idx->device));
+    GS_CUDA(cudaDeviceSynchronize());
+    idx->gen++;
     if (idx->d_kmerx) {
         cudaFree(idx->d_kmerx);
         idx->d_kmerx = NULL;

@@ -23,15 +23,36 @@
  * occ: one 32-byte block per 64 rows of the $-removed BWT string:
  *      {count of A, C, G, T before the block, 4 words of 16 bases, MSB first}.
  * sa:  sampled suffix array, sa[0] = 0xffffffff (the $ row).
- * kmer: (l,u) of every 13-mer, base j at bits 2j, processed first. */
+ * kmer: (l,u) of every 13-mer, base j at bits 2j, processed first.
+ * Optional text structures, all built from occ and sa in HBM:
+ * saf:  the full suffix array, saf[row] for every row 0..seq_len (saf[0] =
+ *       0xffffffff like sa[0]);
+ * text: the reference text T[0..seq_len), 16 bases per word, base i at bits
+ *       2*(i & 15) of word i >> 4, padded by two zero words;
+ * isa:  the row of the suffix at text position j * GS_ISA_STEP, for every
+ *       j * GS_ISA_STEP <= seq_len;
+ * quirk_lo / quirk_n: text positions [quirk_lo, quirk_lo + quirk_n) are the
+ *       rows whose LF walk passes row primary+1 before a sampled row; the LF
+ *       quirk locates them at position - quirk_lo;
+ * text_min: a walker that has taken this many steps with a one-row interval
+ *       and no neighbour interval, with 16 or more bases left, compares the
+ *       read with the text (0: never). */
+#define GS_ISA_STEP 4u
+#define GS_TEXT_MARK 0xf0000000u     /* jl of a text-mode walker */
+#define GS_REGIME_MARK 0xe0000000u   /* jl (+ steps) of a one-row walker without J */
 struct GsDevIndex {
     const uint32_t *occ;
     const uint32_t *sa;
     const uint2 *kmer;
     const uint2 *kmerx;        /* optional (l,u) table of all kx-mers, same bit order */
+    const uint32_t *saf;
+    const uint32_t *text;
+    const uint32_t *isa;
     int32_t kx;                /* 14..16, or 0 when there is no longer table */
     uint32_t primary, seq_len, sa_intv, n_sa;
     uint32_t L2[5];
+    uint32_t quirk_lo, quirk_n;
+    int32_t text_min;
 };
 
 /* Candidate slot written by the search kernels; y == 0 marks "no record". */
@@ -84,7 +105,8 @@ struct GsBatch {
     uint32_t item_cap;             /* work items the hand-over buffer is sized for */
     uint64_t cont_cap;             /* hand-over records allocated */
     uint32_t *queue;           /* [0]: work-queue head, [1]: status flags,
-                                  [2]: hand-over count, [3]: tail-pass head */
+                                  [2]: hand-over count, [3]: tail-pass head,
+                                  [4]: text jobs queued (8 words, zeroed per pass) */
     unsigned long long *work;  /* NULL or [kmer, occ blocks, lf steps, sa samples] */
     GsCont *cont;              /* NULL: no hand-over; else n_items * handoff_lanes entries */
     int32_t handoff_lanes;     /* hand over when at most this many owned lanes extend ... */
@@ -92,6 +114,14 @@ struct GsBatch {
     uint32_t max_occ;          /* 0 or the largest interval an output seed may have */
     GsWalker *walkers;         /* batched search: survivors of the start pass */
     uint64_t walker_cap;       /* entries allocated (0: every walk stays in the start pass) */
+    struct GsTextJob *text_jobs;   /* walkers handed to the text pass */
+    uint64_t text_cap;         /* entries allocated (0: text mode stays inline) */
+};
+
+/* A walker that entered text mode in the walk pass, finished by the text
+ * pass: its read, anchor (| GS_WALKER_FWD), far end and row. */
+struct GsTextJob {
+    uint32_t r, anchor, pos, l;
 };
 
 #define GS_FLAG_WALK 1u
@@ -138,6 +168,9 @@ int gs_build_kmer_table(const GsDevIndex &idx, uint2 *table, cudaStream_t st);
 int gs_launch_text_lengths(const GsTextArgs &a, cudaStream_t st);
 int gs_launch_text_write(const GsTextArgs &a, cudaStream_t st);
 int gs_build_kmerx_table(const GsDevIndex &idx, uint2 *table, int kx, cudaStream_t st);
+/* full SA, text and sampled ISA from occ + sa; GS_EFORMAT when the index
+ * does not describe one text (the structures are then not used) */
+int gs_build_text(GsDevIndex &idx, uint32_t *saf, uint32_t *text, uint32_t *isa, cudaStream_t st);
 /* n_items: host-known work-item count for grid sizing, or 0 (graph capture):
  * the kernels read the count from item_off[n_reads] on the device */
 int gs_launch_search(const GsDevIndex &idx, GsBatch &b, int kernel, int queue_chunk,

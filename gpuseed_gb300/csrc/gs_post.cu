@@ -334,10 +334,19 @@ __global__ void __launch_bounds__(256) gs_locate(GsDevIndex I, const gs_seed_rec
             uint32_t row = S.l + (uint32_t)(j - seed_pos[s]);
             if (S.xl <= S.xu && row >= S.xl) row += S.xu - S.xl + 1u;
             /* locate_seeds_gpu (:668-684): LF until a sampled row; a
-             * consistent index reaches one within seq_len+1 steps */
+             * consistent index reaches one within seq_len+1 steps.  With
+             * the full suffix array it is one read: the walk's result is
+             * SA[row], except that the LF quirk sends the rows whose walk
+             * passes row primary+1 to row 0, where sa[0] = -1 gives the
+             * steps taken minus one -- position - quirk_lo. */
             const uint32_t cap = I.seq_len + 2u;
             bool bad = false;
-            while (row % I.sa_intv) {
+            if (I.saf) {
+                uint32_t v = __ldg(&I.saf[row]);
+                if (lf_mode == GS_LF_GPUSEED && v - I.quirk_lo < I.quirk_n) v -= I.quirk_lo;
+                out[j] = v;
+            }
+            while (!I.saf && row % I.sa_intv) {
                 row = gs_lf(I, row, lf_mode);
                 if (++steps > cap) {
                     bad = true;
@@ -347,7 +356,7 @@ __global__ void __launch_bounds__(256) gs_locate(GsDevIndex I, const gs_seed_rec
             if (bad) {
                 atomicOr(flags, GS_FLAG_WALK);
                 out[j] = 0xffffffffu;
-            } else {
+            } else if (!I.saf) {
                 out[j] = __ldg(&I.sa[row / I.sa_intv]) + steps;
             }
         }

@@ -544,22 +544,131 @@ __global__ void __launch_bounds__(256, 5) gs_search_lockstep(GsDevIndex I, GsBat
 #define GS_WALKER_CHUNK 512u      /* buffer entries a warp reserves at a time */
 #define GS_WALK_WINDOW 256u       /* buffer entries a walk-pass warp takes at a time */
 
+/* Text mode.  A walker whose interval is one row [l,l] and whose J is
+ * empty can no longer be contained: its walk only extends one occurrence,
+ * at text position q = SA[l], while the read goes on matching T[q-1],
+ * T[q-2], ...  It ends where the read and the text differ, the read or the
+ * text ends, or (GS_N_STOP) a non-ACGT base comes; its record is the row of
+ * the suffix at that position.  Text mode finds that position by comparing
+ * 16 bases a round and takes its row from the inverse-SA sample at or above
+ * it, with at most GS_ISA_STEP-1 LF steps over the text bases in between.
+ * Under GS_N_WILDCARD a non-ACGT base hands the walker back to the
+ * interval walk, which skips the base.  The walker's J words hold the
+ * state: jl = GS_TEXT_MARK | phase << 26 | flags, ju = a text position. */
+#define GS_TM_MOVED (1u << 25)   /* the compare advanced past the entry position */
+#define GS_TM_CONT (1u << 24)    /* a wildcard base follows: back to the interval walk */
+
+template <int COUNT>
+__device__ __forceinline__ bool gs_text_round(const GsDevIndex &I, const unsigned char *seq, int iL,
+                                              bool fwd, int dir, uint32_t &l, uint32_t &u,
+                                              uint32_t &jl, uint32_t &ju, int &pos, int nstop,
+                                              unsigned long long &wb)
+{
+    const uint32_t ph = (jl >> 26) & 3u;
+    (void)wb;
+    if (ph == 0) {
+        ju = __ldg(&I.saf[l]);
+        jl = GS_TEXT_MARK | (1u << 26);
+        return true;
+    }
+    bool cont;
+    if (ph == 1) {
+        const uint32_t q = ju;
+        const int rem = fwd ? pos : iL - 1 - pos;
+        int avail = rem < 16 ? rem : 16;
+        if ((uint32_t)avail > q) avail = (int)q;
+        int m = 0, bad = avail;
+        if (avail > 0) {
+            /* T[q-16..q-1], T[q-1] at bits 30-31 */
+            uint32_t wt;
+            if (q >= 16) {
+                const uint32_t b = q - 16u;
+                wt = __funnelshift_r(__ldg(&I.text[b >> 4]), __ldg(&I.text[(b >> 4) + 1]),
+                                     (b & 15u) << 1);
+            } else {
+                wt = __ldg(&I.text[0]) << ((16u - q) << 1);
+            }
+            /* the read's next bases in walk order, the first at bits 30-31 */
+            uint32_t wr = 0;
+#pragma unroll 1
+            for (int i = 0; i < avail; i++) {
+                const unsigned char ch = seq[pos + dir * (i + 1)];
+                const uint32_t c = fwd ? gs_fwd_code(ch) : gs_comp_code(ch);
+                if (c > 3u && bad == avail) bad = i;
+                wr |= (c & 3u) << (30 - 2 * i);
+            }
+            m = (int)(__clz(wr ^ wt) >> 1);
+            if (m > bad) m = bad;
+            pos += dir * m;
+            ju = q - (uint32_t)m;
+            if (m) jl |= GS_TM_MOVED;
+            if (m == avail && avail < rem && ju > 0u) return true;
+        }
+        cont = !nstop && m == bad && bad < avail;
+        if (!(jl & GS_TM_MOVED)) {
+            /* still at the entry row */
+            if (!cont) return false;
+            jl = 1u;
+            ju = 0u;
+            return true;
+        }
+        jl = GS_TEXT_MARK | (2u << 26) | (cont ? GS_TM_CONT : 0u);
+        return true;
+    }
+    cont = (jl & GS_TM_CONT) != 0;
+    {
+        /* the row of position qs from the sample at qp >= qs (position
+         * seq_len is row 0), and T[qs..qs+3] for the LF steps down to qs */
+        const uint32_t qs = ju;
+        uint32_t qp = (qs + GS_ISA_STEP - 1u) & ~(GS_ISA_STEP - 1u);
+        uint32_t row = 0;
+        if (qp > I.seq_len) qp = I.seq_len;
+        else row = __ldg(&I.isa[qp / GS_ISA_STEP]);
+        const uint32_t w = __funnelshift_r(__ldg(&I.text[qs >> 4]), __ldg(&I.text[(qs >> 4) + 1]),
+                                           (qs & 15u) << 1);
+        l = u = row;
+        const uint32_t d = qp - qs;
+        jl = GS_TEXT_MARK | (3u << 26) | (jl & GS_TM_CONT) | (d << 16) | (w & 0xffu);
+        if (d) return true;
+    }
+    /* phase 3, the LF steps, is the interval walk's own step (gs_walk_step) */
+    if (!cont) return false;
+    jl = 1u;
+    ju = 0u;
+    return true;
+}
+
 /* One iteration of a walk: normally a step of I and J with the next
  * base; for a walker whose J is still one base short (jpend), the J-only
  * step with the base at pos that brings J to I's far end -- the same call,
  * so the lanes of a warp take one memory round per iteration either way.
- * Returns false when the walk is over (killed: it ended by containment). */
-template <int NSTOP, int COUNT>
+ * Returns false when the walk is over (killed: it ended by containment).
+ * A step that leaves the walker eligible for text mode sets jl to
+ * GS_TEXT_MARK. */
+template <int NSTOP, int COUNT, bool TEXT>
 __device__ __forceinline__ bool gs_walk_step(const GsDevIndex &I, const unsigned char *seq, int iL,
                                              bool fwd, int dir, uint32_t &l, uint32_t &u,
                                              uint32_t &jl, uint32_t &ju, int &pos, bool &jpend,
                                              bool &killed, unsigned long long &wb)
 {
-    const bool settle = jpend;
-    jpend = false;
-    const int np = settle ? pos : pos + dir;
-    if (np < 0 || np >= iL) return false;
-    const uint32_t c = fwd ? gs_fwd_code(seq[np]) : gs_comp_code(seq[np]);
+    /* TEXT: text-mode states run here; otherwise the caller hands a walker
+     * that enters text mode to the text pass */
+    const bool text = TEXT && jl >= GS_TEXT_MARK;
+    bool settle = false;
+    int np = pos;
+    uint32_t c;
+    if (text) {
+        if (((jl >> 26) & 3u) != 3u)
+            return gs_text_round<COUNT>(I, seq, iL, fwd, dir, l, u, jl, ju, pos, NSTOP, wb);
+        /* text mode's LF step with base T[qs + d - 1]; J stays empty */
+        c = (jl >> ((((jl >> 16) & 15u) - 1u) << 1)) & 3u;
+    } else {
+        settle = jpend;
+        jpend = false;
+        np = settle ? pos : pos + dir;
+        if (np < 0 || np >= iL) return false;
+        c = fwd ? gs_fwd_code(seq[np]) : gs_comp_code(seq[np]);
+    }
     if (c > 3u) {
         if (!settle) {
             if (NSTOP) return false;
@@ -571,6 +680,17 @@ __device__ __forceinline__ bool gs_walk_step(const GsDevIndex &I, const unsigned
         uint32_t nl = l, nu = u;
         int blocks = gs_step_pair(I, nl, nu, jl, ju, c, !settle);
         if (COUNT) wb += (unsigned long long)blocks;
+        if (text) {
+            l = nl;
+            u = nu;
+            const uint32_t d = ((jl >> 16) & 15u) - 1u;
+            jl = (jl & ~(15u << 16)) | (d << 16);
+            if (d) return true;
+            if (!(jl & GS_TM_CONT)) return false;
+            jl = 1u;
+            ju = 0u;
+            return true;
+        }
         if (!settle) {
             if (nl > nu) return false;   /* natural end at pos */
             l = nl;
@@ -581,6 +701,18 @@ __device__ __forceinline__ bool gs_walk_step(const GsDevIndex &I, const unsigned
     if (jl <= ju && ju - jl == u - l) {
         killed = true;
         return false;
+    }
+    /* one row and no J: count the steps taken so (J's words are free);
+     * after text_min of them the occurrence is no chance hit, and with 16
+     * bases or more left the walker enters text mode */
+    if (I.text_min && l == u && jl > ju) {
+        if (jl < GS_REGIME_MARK) {
+            jl = GS_REGIME_MARK;
+            ju = 0u;
+        } else if (++jl - GS_REGIME_MARK >= (uint32_t)I.text_min &&
+                   (fwd ? pos : iL - 1 - pos) >= 16) {
+            jl = GS_TEXT_MARK;
+        }
     }
     return true;
 }
@@ -598,7 +730,8 @@ __device__ __noinline__ void gs_walk_in_place(const GsDevIndex &I, const GsBatch
     const int iL = (int)B.lengths[r];
     const int dir = fwd ? -1 : 1;
     bool killed = false;
-    while (gs_walk_step<NSTOP, COUNT>(I, seq, iL, fwd, dir, l, u, jl, ju, pos, jpend, killed, wb)) {
+    while (gs_walk_step<NSTOP, COUNT, true>(I, seq, iL, fwd, dir, l, u, jl, ju, pos, jpend, killed,
+                                            wb)) {
     }
     gs_write_record(B, r, n, fwd, anchor, pos, l, u, true, killed);
 }
@@ -743,10 +876,12 @@ __global__ void __launch_bounds__(128, 8) gs_search_walk(GsDevIndex I, GsBatch B
     const int lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
     unsigned long long wb = 0;
-    uint64_t n_w = *(volatile uint32_t *)(B.queue + 2);
-    if (n_w > B.walker_cap) n_w = B.walker_cap;
-    uint64_t win = 0, win_end = 0;   /* warp-uniform window of walker indices */
+    /* walker indices fit 32 bits: the buffer holds at most 2^31 entries */
+    uint32_t n_w = *(volatile uint32_t *)(B.queue + 2);
+    if (n_w > B.walker_cap) n_w = (uint32_t)B.walker_cap;
+    uint32_t win = 0, win_end = 0;   /* warp-uniform window of walker indices */
     bool have = false, exhausted = false, killed = false, jpend = false;
+    bool tfull = B.text_cap == 0;   /* warp-uniform: the text-job buffer is full */
     uint32_t r = 0, l = 0, u = 0, jl = 0, ju = 0, n = 0;
     int anchor = 0, pos = 0, iL = 0, dir = 0;
     bool fwd = false;
@@ -763,9 +898,9 @@ __global__ void __launch_bounds__(128, 8) gs_search_walk(GsDevIndex I, GsBatch B
                     break;
                 }
                 win = g;
-                win_end = min((uint64_t)g + GS_WALK_WINDOW, n_w);
+                win_end = min(g + GS_WALK_WINDOW, n_w);
             }
-            const uint32_t take = (uint32_t)min((uint64_t)__popc(need), win_end - win);
+            const uint32_t take = min((uint32_t)__popc(need), win_end - win);
             const uint32_t rank = __popc(need & lt);
             if (((need >> lane) & 1u) && rank < take) {
                 GsWalker w = B.walkers[win + rank];
@@ -796,11 +931,69 @@ __global__ void __launch_bounds__(128, 8) gs_search_walk(GsDevIndex I, GsBatch B
             if (exhausted) break;
             continue;
         }
-        if (have &&
-            !gs_walk_step<NSTOP, COUNT>(I, seq, iL, fwd, dir, l, u, jl, ju, pos, jpend, killed, wb)) {
+        if (have && !gs_walk_step<NSTOP, COUNT, false>(I, seq, iL, fwd, dir, l, u, jl, ju, pos,
+                                                       jpend, killed, wb)) {
             gs_write_record(B, r, n, fwd, anchor, pos, l, u, true, killed);
             have = false;
         }
+        /* walkers that entered text mode go to the text pass, so that no
+         * lane of this pass runs the compare; without room they walk on */
+        const bool tx = have && jl >= GS_TEXT_MARK;
+        const uint32_t tm = __ballot_sync(0xffffffffu, tx);
+        if (tm) {
+            uint32_t g = 0xffffffffu;
+            if (!tfull) {
+                const int lead = __ffs(tm) - 1;
+                if (lane == lead) g = atomicAdd(B.queue + 4, (uint32_t)__popc(tm));
+                g = __shfl_sync(0xffffffffu, g, lead);
+                if ((uint64_t)g + __popc(tm) > B.text_cap) tfull = true;
+            }
+            const uint64_t idx = (uint64_t)g + __popc(tm & lt);
+            if (tx) {
+                if (g != 0xffffffffu && idx < B.text_cap) {
+                    GsTextJob t;
+                    t.r = r;
+                    t.anchor = (uint32_t)anchor | (fwd ? GS_WALKER_FWD : 0u);
+                    t.pos = (uint32_t)pos;
+                    t.l = l;
+                    B.text_jobs[idx] = t;
+                    have = false;
+                } else {
+                    jl = 1u;
+                    ju = 0u;
+                }
+            }
+        }
+    }
+    if (COUNT) gs_add_work(B, 0, wb);
+}
+
+/* Text pass: the walkers the walk pass handed over, one per thread, each
+ * run to its end in text mode (and back in the interval walk after a
+ * wildcard base). */
+template <int NSTOP, int COUNT>
+__global__ void __launch_bounds__(256) gs_search_text(GsDevIndex I, GsBatch B)
+{
+    uint64_t n_jobs = B.queue[4];
+    if (n_jobs > B.text_cap) n_jobs = B.text_cap;
+    unsigned long long wb = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n_jobs; j += stride) {
+        const GsTextJob t = B.text_jobs[j];
+        const uint32_t r = t.r;
+        const bool fwd = (t.anchor & GS_WALKER_FWD) != 0;
+        const int anchor = (int)(t.anchor & ~GS_WALKER_FWD);
+        const int dir = fwd ? -1 : 1;
+        const uint32_t Lr = B.lengths[r];
+        const int iL = (int)Lr;
+        const unsigned char *seq = (const unsigned char *)B.seqs + B.offsets[r];
+        int pos = (int)t.pos;
+        uint32_t l = t.l, u = t.l, jl = GS_TEXT_MARK, ju = 0u;
+        bool jpend = false, killed = false;
+        while (gs_walk_step<NSTOP, COUNT, true>(I, seq, iL, fwd, dir, l, u, jl, ju, pos, jpend,
+                                                killed, wb)) {
+        }
+        gs_write_record(B, r, Lr - (uint32_t)B.k + 1u, fwd, anchor, pos, l, u, true, killed);
     }
     if (COUNT) gs_add_work(B, 0, wb);
 }
@@ -929,6 +1122,13 @@ static int gs_launch_batched(const GsDevIndex &I, GsBatch &B, int queue_chunk, i
         GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&wocc, walk, 128, 0));
         walk<<<(uint32_t)sms * (uint32_t)(wocc > 0 ? wocc : 4), 128, 0, st>>>(I, B);
         GS_CUDA(cudaGetLastError());
+        if (B.text_cap) {
+            void (*text)(GsDevIndex, GsBatch) =
+                nstop ? (cnt ? gs_search_text<1, 1> : gs_search_text<1, 0>)
+                      : (cnt ? gs_search_text<0, 1> : gs_search_text<0, 0>);
+            text<<<(uint32_t)sms * 8u, 256, 0, st>>>(I, B);
+            GS_CUDA(cudaGetLastError());
+        }
     }
     return GS_OK;
 }

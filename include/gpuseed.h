@@ -103,6 +103,9 @@ typedef struct {
     int32_t device;
     uint64_t device_bytes;          /* HBM held by the index */
     int32_t kmer_len;               /* start-table length in use (13..16) */
+    int32_t text_min;               /* text structures: > 0 the min_steps of
+                                       gs_index_set_text, -1 built but text mode off,
+                                       0 not built */
 } gs_index_info;
 
 /* ---- index -------------------------------------------------------------
@@ -134,6 +137,24 @@ int gs_index_build(const uint8_t *codes, uint64_t n, uint32_t sa_intv, int devic
  * SA interval of a string does not depend on how it is found, so results do
  * not change; seeding uses it only when k > len. */
 int gs_index_set_kmer_len(gs_index *idx, int kmer_len);
+/* Text structures in HBM, built from the .bwt and .sa by one pass of LF
+ * chains (4 * seq_len bytes of full suffix array, seq_len / 4 of packed text,
+ * seq_len of inverse-SA samples every 4 positions; loading builds them when
+ * the memory is there, with min_steps 4).  With them, locate reads each
+ * position from the full suffix array instead of walking to a sampled row,
+ * and a walker whose interval has been one row, with its containment test
+ * over, for min_steps steps (so that the row is the read's own locus, not a
+ * chance hit) compares its read with the text, 16 bases a step, in a pass
+ * of its own; it takes the row where the match ends from the inverse-SA
+ * samples.  Seeds and positions do not change.  min_steps > 0: build if
+ * needed and use both; < 0: build if needed, locate only; 0: free them.
+ * Call while no pass runs on a context of this index. */
+int gs_index_set_text(gs_index *idx, int min_steps);
+/* Copies entries [first, first+count) of a text structure to host memory:
+ * which 0 = full suffix array (seq_len+1 rows), 1 = packed text words
+ * (ceil(seq_len/16)), 2 = inverse-SA samples (seq_len/4 + 1). */
+int gs_index_text_table(const gs_index *idx, int which, uint64_t first, uint64_t count,
+                        uint32_t *out);
 /* Keeps the occurrence table in L2 under an access-policy window on the
  * streams of contexts created afterwards (fraction of the set-aside; 0, the
  * default, disables it and releases the set-aside).  Measured slower on the
@@ -186,6 +207,9 @@ int gs_ctx_last_work(gs_ctx *ctx, uint64_t out[4]);
  * start pass handed to the walk pass, and the walker buffer's capacity
  * (handed beyond it: walked in the start pass instead). */
 int gs_ctx_last_walkers(gs_ctx *ctx, uint64_t *n_walkers, uint64_t *capacity);
+/* Walkers the last batched pass handed to its text pass, and the room it had
+ * for them (0, 0 without text mode). */
+int gs_ctx_last_text_jobs(gs_ctx *ctx, uint64_t *n_jobs, uint64_t *capacity);
 
 /* ---- autotuner ----------------------------------------------------------
  * Times the search on the first `sample` reads (device buffers) by coordinate

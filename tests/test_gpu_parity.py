@@ -64,13 +64,13 @@ def test_random_reads(small, kernel, smem, n_mode):
             assert_same(gres, ob, len(reads), f"k={k} lf={lf}")
 
 
-def test_edge_cases(small):
+def edge_reads(small):
     codes = small["codes"]
     text = "".join("ACGT"[c] for c in codes)
     sa = pyoracle.suffix_array(codes)
     primary = small["oidx"].primary
     q = int(sa[primary + 1])      # text position whose row is primary+1 (LF quirk)
-    reads = [
+    return [
         b"",                                   # empty read
         b"ACGT",                               # shorter than k
         text[1000:1020].encode(),              # exactly k
@@ -87,6 +87,10 @@ def test_edge_cases(small):
         text[:120].encode(), text[-120:].encode(),
         b"ACGTRYKMSWBDHV@X" * 4,               # other letters (codes 0 and 5)
     ]
+
+
+def test_edge_cases(small):
+    reads = edge_reads(small)
     seqs, offs, lens = pack(reads)
     for kernel in (0, 1, 2):
         for smem in (False, True):
@@ -96,6 +100,95 @@ def test_edge_cases(small):
                                              kernel=kernel)
                     ob = small["oidx"].seed(seqs, offs, lens, k=k, smem=smem, lf_mode=lf)
                     assert_same(gres, ob, len(reads), f"edge kernel={kernel} smem={smem} lf={lf} k={k}")
+
+
+def test_text_structures(small):
+    """The full suffix array, packed text and inverse-SA samples that loading
+    builds in HBM from the .bwt and .sa equal the oracle's suffix array and
+    the text."""
+    gidx = small["gidx"]
+    assert gidx.info().text_min > 0
+    codes = small["codes"]
+    n = codes.size
+    sa = pyoracle.suffix_array(codes)
+    want = sa.copy()
+    want[0] = 0xffffffff                  # row 0 keeps the sa[0] sentinel
+    assert np.array_equal(gidx.text_table(0), want)
+    padded = np.zeros(((n + 15) // 16) * 16, np.uint32)
+    padded[:n] = codes
+    words = np.bitwise_or.reduce(padded.reshape(-1, 16) << (2 * np.arange(16, dtype=np.uint32)),
+                                 axis=1)
+    assert np.array_equal(gidx.text_table(1), words.astype(np.uint32))
+    isa = np.empty(n + 1, np.int64)
+    isa[sa.astype(np.int64)] = np.arange(n + 1)
+    assert np.array_equal(gidx.text_table(2), isa[::4].astype(np.uint32))
+
+
+def text_mode_reads(small):
+    """Long exact copies (text mode runs far), copies with a wildcard or a
+    substitution mid-way, copies at both ends of the text, random reads."""
+    codes = small["codes"]
+    text = "".join("ACGT"[c] for c in codes)
+    n = len(text)
+    rng = np.random.default_rng(5)
+    reads = edge_reads(small)
+    for L in (40, 90, 160, 300):
+        for _ in range(6):
+            a = int(rng.integers(0, n - L))
+            s = text[a:a + L]
+            reads.append(s.encode())
+            j = int(rng.integers(5, L - 5))
+            reads.append((s[:j] + "N" + s[j + 1:]).encode())
+            reads.append((s[:j] + "ACGT"[("ACGT".index(s[j]) + 1) % 4] + s[j + 1:]).encode())
+            reads.append((s[:j] + "NN" + s[j + 2:]).lower().encode())
+        reads.append(text[:L].encode())
+        reads.append(text[n - L:].encode())
+        reads.append((text[:L // 2] + "N" + text[L // 2 + 1:L]).encode())
+    reads += sample_reads(codes, 200, seed=73, lengths=(20, 33, 64, 100, 150, 300), err=0.01)
+    return reads
+
+
+@pytest.mark.parametrize("text_min", [1, 5, 16, -1, 0], ids=["t1", "t5", "t16", "locate", "off"])
+def test_text_mode(small, text_min):
+    """Text mode at several entry thresholds, the full-SA locate alone, and
+    neither: every kernel, both modes, both N and LF modes, and every walk in
+    the start pass (walker_slots < 0) give the oracle's seeds and positions."""
+    gs = _gs()
+    gidx = gs.Index(small["prefix"])
+    gidx.set_text(text_min)
+    assert gidx.info().text_min == (text_min if text_min > 0 else text_min and -1)
+    ctx = gs.Context(gidx)
+    reads = text_mode_reads(small)
+    seqs, offs, lens = pack(reads)
+    for kernel, slots in ((0, 0), (0, -1), (1, 0), (2, 0)):
+        for smem in (False, True):
+            for n_mode in (0, 1):
+                for lf in (0, 1):
+                    gres = ctx.seed(seqs, offs, lens, k=19, smem=smem, n_mode=n_mode, lf_mode=lf,
+                                    kernel=kernel, walker_slots=slots)
+                    ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=smem, n_mode=n_mode,
+                                            lf_mode=lf)
+                    assert_same(gres, ob, len(reads),
+                                f"text_min={text_min} kernel={kernel}/{slots} smem={smem} "
+                                f"n_mode={n_mode} lf={lf}")
+
+
+def test_text_build_checks_samples(small):
+    """An .sa whose samples do not continue the BWT's chains gets no text
+    structures (GS_EFORMAT); the index still loads and seeds by LF walks."""
+    gs = _gs()
+    prefix = small["prefix"]
+    bwt = np.fromfile(prefix + ".bwt", dtype=np.uint32)
+    sa = np.fromfile(prefix + ".sa", dtype=np.uint32)
+    samples = sa[7:].copy()
+    samples[[3, 4]] = samples[[4, 3]]
+    gidx = gs.Index(arrays=(int(bwt[0]), bwt[1:5], bwt[5:], samples, int(sa[5])))
+    assert gidx.info().text_min == 0
+    with pytest.raises(gs.GsError) as e:
+        gidx.set_text(24)
+    assert e.value.code == -3        # GS_EFORMAT
+    ok = gs.Index(arrays=(int(bwt[0]), bwt[1:5], bwt[5:], sa[7:], int(sa[5])))
+    assert ok.info().text_min > 0
 
 
 def test_empty_batch(small):
@@ -184,17 +277,26 @@ def test_config1_full(built, tmp_path_factory):
 
 def test_work_counters_match_oracle(small):
     """The plain kernel's containment-stopped walk does exactly the oracle's
-    canonical work (13-mer lookups, occurrence blocks, LF steps, SA samples)."""
+    canonical work (13-mer lookups, occurrence blocks, LF steps, SA samples)
+    on an index without text structures; with them, locate reads the full
+    suffix array once per position and takes no LF steps."""
+    gs = _gs()
     reads = sample_reads(small["codes"], 300, seed=21, lengths=(50, 100, 150, 250))
     seqs, offs, lens = pack(reads)
+    bare = gs.Index(small["prefix"])
+    bare.set_text(0)
+    ctx = gs.Context(bare)
     for smem in (False, True):
-        small["ctx"].seed(seqs, offs, lens, k=19, smem=smem, kernel=1, count_work=True)
-        w = small["ctx"].last_work()
+        ctx.seed(seqs, offs, lens, k=19, smem=smem, kernel=1, count_work=True)
+        w = ctx.last_work()
         ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=smem, pruned=True)
         assert w["n_kmer"] == ob.work["n_kmer"]
         assert w["n_occ_blocks"] == ob.work["n_occ_blocks"]
         assert w["n_lf"] == ob.work["n_lf"]
         assert w["n_sa"] == ob.work["n_sa"]
+        small["ctx"].seed(seqs, offs, lens, k=19, smem=smem, kernel=1, count_work=True)
+        wt = small["ctx"].last_work()
+        assert wt["n_lf"] == 0 and wt["n_sa"] == ob.work["n_sa"]
 
 
 @pytest.mark.parametrize("kx", [14, 16])
