@@ -341,11 +341,18 @@ def run_reference_arm(args):
 
 def config_dict(args, w, sample_note=None):
     spec = w["spec"]
+    if w.get("idx") is not None:
+        info = w["idx"].info()
+        index_gb = (f"{info.device_bytes / 1e9:.1f} GB on the device, "
+                    f"text structures {'on' if info.text_min else 'off'}")
+    else:
+        index_gb = "files in host memory"
     d = {"workload": f"config {args.config}: {spec.length / 1e9:.2f} Gbp synthetic reference, "
                      f"{w['lens'].size:,} reads {'SMEM' if w['smem'] else 'MEM'} k={w['k']}",
          "ref_bp": int(spec.length), "reads": int(w["lens"].size), "bases": int(w["lens"].sum()),
          "k": w["k"], "mode": "smem" if w["smem"] else "mem", "sa_intv": 7,
-         "l2": "inputs larger than L2 (reads 1.25 GB, index 3.8 GB); no flush"}
+         "l2": f"inputs larger than L2 (reads {w['lens'].sum() / 1e9:.2f} GB, index "
+               f"{index_gb}); no flush"}
     if sample_note:
         d["sample"] = sample_note
     return d
@@ -463,6 +470,7 @@ def main():
         search_ms.append(ctx.last_timing()[0])
     search_ms = search_ms[1:]
     walkers, walker_cap = ctx.last_walkers()
+    text_jobs, text_cap = ctx.last_text_jobs()
     # the lockstep form of the batched search, same pipeline otherwise
     lock_ms = []
     for _ in range(3):
@@ -523,7 +531,7 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
                 "peak_source": f"{peak_src} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
-                "kernel": "gs_search_start + gs_search_walk (one search pass)",
+                "kernel": "gs_search_start + gs_search_walk + gs_search_text (one search pass)",
                 "algorithmic_bytes_per_launch": search_bytes,
                 "random_32B_gather_gbs": g32.value,
                 "frac_of_random_32B": achieved / g32.value if g32.value else None}
@@ -605,7 +613,8 @@ def main():
             "seeds_per_step": n_seeds, "positions_per_step": n_pos,
             "lockstep": {"search_ms": statistics.mean(lock_ms), "knobs": {"queue_chunk": 16,
                          "handoff_lanes": 2, "handoff_steps": 6}},
-            "walkers": {"handed_to_walk_pass": walkers, "buffer": walker_cap},
+            "walkers": {"handed_to_walk_pass": walkers, "buffer": walker_cap,
+                        "handed_to_text_pass": text_jobs, "text_buffer": text_cap},
             "text": text,
             "work": work,
             "work_executed_batched": {"n_kmer": executed["n_kmer"],
@@ -614,7 +623,8 @@ def main():
                                       max(1, work["n_kmer"] + work["n_occ_blocks"])},
             "e2e": {"value": e2e_value, "unit": "reads/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": 7 * args.steps,
+            # prepare, start, walk, (text), finalize count + emit, expand, locate
+            "gpu_launches": (8 if idx.info().text_min > 0 else 7) * args.steps,
             "graph": "each timed step replays one CUDA graph of the whole pass",
             "clocks": clocks.summary(),
             "roofline": roofline,
