@@ -569,6 +569,10 @@ def main():
     # the -o records of this result: GPU formatting vs the host writer, to /dev/null
     text = None
     if not args.no_text:
+        # a device-resident pass leaves the result on both sides (gs_seed in
+        # chunks keeps the host result only)
+        ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), n_reads,
+                        fetch=True, k=k, smem=smem, **knobs)
         fd = os.open(os.devnull, os.O_WRONLY)
         try:
             ctx.text_device(1, smem)

@@ -16,6 +16,9 @@
  */
 #include "gs_internal.h"
 
+#define GS_SEED_CHUNK_READS (1u << 21)   /* gs_seed runs batches of twice this in chunks */
+#define GS_SEED_MAX_CHUNKS 16
+
 #include <cub/cub.cuh>
 
 #include <atomic>
@@ -100,6 +103,16 @@ static int grow(T *&p, size_t &cap, size_t n, cudaStream_t st)
     return GS_OK;
 }
 
+/* One chunk of a gs_seed batch: where its results go in the batch's host
+ * arrays, and what it found. */
+struct GsChunkOut {
+    uint32_t first_read;      /* the chunk's first read in the batch */
+    uint64_t base_s, base_p;  /* seeds and positions of the chunks before it */
+    double scale;             /* batch reads / chunk reads, to size the host arrays once */
+    int wait_d2h;             /* the previous chunk's copy-out may still run */
+    uint64_t n_seeds, n_pos;  /* out */
+};
+
 template <class T>
 static int grow_host(T *&p, size_t &cap, size_t n)
 {
@@ -114,6 +127,24 @@ static int grow_host(T *&p, size_t &cap, size_t n)
     return GS_OK;
 }
 
+/* grow_host keeping the first `keep` entries, once the copies on `busy`
+ * that write into the old array are done */
+template <class T>
+static int grow_host_keep(T *&p, size_t &cap, size_t n, size_t keep, cudaStream_t busy)
+{
+    if (n <= cap && p) return GS_OK;
+    GS_CUDA(cudaStreamSynchronize(busy));
+    size_t nc = n + n / 4 + 64;
+    T *np = NULL;
+    cudaError_t e = cudaMallocHost(&np, nc * sizeof(T));
+    if (e != cudaSuccess) return gs_cuda_fail(e, "cudaMallocHost(result)");
+    if (keep && p) memcpy(np, p, keep * sizeof(T));
+    cudaFreeHost(p);
+    p = np;
+    cap = nc;
+    return GS_OK;
+}
+
 struct gs_ctx {
     gs_index *idx;
     cudaStream_t st;
@@ -121,6 +152,11 @@ struct gs_ctx {
     cudaEvent_t ev0, ev_s0, ev_s1, ev1;
     cudaStream_t st_copy;       /* copies seeds out while positions are located */
     cudaEvent_t ev_emit;
+    /* gs_seed in chunks: reads go up on st_h2d, each chunk's results come
+     * down on st_copy while the next chunk runs on st */
+    cudaStream_t st_h2d;
+    cudaEvent_t ev_h2d[GS_SEED_MAX_CHUNKS];
+    cudaEvent_t ev_done, ev_d2h;
     /* inputs staged by gs_seed_rec */
     char *d_seqs; size_t cap_seqs;
     uint64_t *d_offsets; size_t cap_offsets;
@@ -198,6 +234,11 @@ extern "C" int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out)
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st_copy, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_emit, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st_h2d, cudaStreamNonBlocking);
+    for (int i = 0; i < GS_SEED_MAX_CHUNKS && e == cudaSuccess; i++)
+        e = cudaEventCreateWithFlags(&c->ev_h2d[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_d2h, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&c->queue, 32);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_max, 16);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_work, 32);
@@ -274,6 +315,14 @@ extern "C" void gs_ctx_free(gs_ctx *c)
         cudaStreamSynchronize(c->st_copy);
         cudaStreamDestroy(c->st_copy);
     }
+    if (c->st_h2d) {
+        cudaStreamSynchronize(c->st_h2d);
+        cudaStreamDestroy(c->st_h2d);
+    }
+    for (int i = 0; i < GS_SEED_MAX_CHUNKS; i++)
+        if (c->ev_h2d[i]) cudaEventDestroy(c->ev_h2d[i]);
+    if (c->ev_done) cudaEventDestroy(c->ev_done);
+    if (c->ev_d2h) cudaEventDestroy(c->ev_d2h);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     if (c->own_stream && c->st) cudaStreamDestroy(c->st);
     free(c);
@@ -312,17 +361,48 @@ extern "C" int gs_ctx_last_timing(gs_ctx *c, float *search_ms, float *total_ms)
     return GS_OK;
 }
 
-/* end of the longest read, for the plain kernel's per-base history */
+/* end of the longest read, for the plain kernel's per-base history; out[1]
+ * becomes non-zero when a read does not end at or before the next one's
+ * start (gs_seed then copies the reads up whole, not in chunks) */
 __global__ void gs_max_end_kernel(const uint64_t *off, const uint32_t *len, uint32_t n,
                                   unsigned long long *out)
 {
     uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long e = r < n ? (unsigned long long)(off[r] + len[r]) : 0ull;
+    const bool disorder = r + 1 < n && e > off[r + 1];
+    if (__any_sync(0xffffffffu, disorder) && (threadIdx.x & 31) == 0) atomicOr(&out[1], 1ull);
     for (int o = 16; o > 0; o >>= 1) {
         unsigned long long t = __shfl_xor_sync(0xffffffffu, e, o);
         e = t > e ? t : e;
     }
     if ((threadIdx.x & 31) == 0 && e) atomicMax(out, e);
+}
+
+/* Device scalars into the pinned scalar block, written by a kernel: pinned
+ * host memory is mapped into the device's address space under unified
+ * addressing, and a read that takes no copy engine never queues behind a
+ * large copy-out on another stream. */
+__global__ void gs_fetch_small_kernel(uint32_t *dst, const uint32_t *src, uint32_t n_words)
+{
+    if (threadIdx.x < n_words) dst[threadIdx.x] = src[threadIdx.x];
+}
+
+static int fetch_small(uint64_t *dst, const void *src, size_t bytes, cudaStream_t st)
+{
+    gs_fetch_small_kernel<<<1, 32, 0, st>>>((uint32_t *)dst, (const uint32_t *)src,
+                                            (uint32_t)(bytes / 4));
+    GS_CUDA(cudaGetLastError());
+    return GS_OK;
+}
+
+/* a chunk's per-read offsets made batch-wide */
+__global__ void gs_add_base_kernel(uint64_t *seed_off, uint64_t *pos_off, uint32_t n, uint64_t bs,
+                                   uint64_t bp)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        seed_off[i] += bs;
+        pos_off[i] += bp;
+    }
 }
 
 template <class In, class Out>
@@ -369,9 +449,13 @@ static int check_params(const gs_params *p)
         if (_rc) return _rc;     \
     } while (0)
 
+/* One pass over n_reads device-resident reads.  fetch: copy the result to
+ * the context's host arrays.  co (gs_seed's chunks): instead, copy this
+ * chunk's result into the batch's host arrays on st_copy, batch-wide, and
+ * return without waiting for that copy. */
 static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets,
                         const uint32_t *d_lengths, uint32_t n_reads, const gs_params *p,
-                        int fetch)
+                        int fetch, GsChunkOut *co = NULL)
 {
     const GsDevIndex &I = *gs_index_dev(c->idx);
     cudaStream_t st = c->st;
@@ -414,14 +498,14 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     RC(exclusive_scan(c, c->item_cnt, c->item_off, nr1));
     B.slot_off = c->slot_off;
     B.item_off = c->item_off;
-    GS_CUDA(cudaMemcpyAsync(&c->h_small[0], c->slot_off + n_reads, 8, cudaMemcpyDeviceToHost, st));
-    GS_CUDA(cudaMemcpyAsync(&c->h_small[1], c->item_off + n_reads, 4, cudaMemcpyDeviceToHost, st));
+    RC(fetch_small(&c->h_small[0], c->slot_off + n_reads, 8, st));
+    RC(fetch_small(&c->h_small[1], c->item_off + n_reads, 4, st));
     if (p->kernel == GS_KERNEL_PLAIN) {
         GS_CUDA(cudaMemsetAsync(c->d_max, 0, 8, st));
         if (n_reads)
             gs_max_end_kernel<<<(n_reads + 255) / 256, 256, 0, st>>>(
                 d_offsets, d_lengths, n_reads, (unsigned long long *)c->d_max);
-        GS_CUDA(cudaMemcpyAsync(&c->h_small[2], c->d_max, 8, cudaMemcpyDeviceToHost, st));
+        RC(fetch_small(&c->h_small[2], c->d_max, 8, st));
     }
     GS_CUDA(cudaStreamSynchronize(st));
     uint64_t n_slots = c->h_small[0];
@@ -474,6 +558,9 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     GS_CUDA(cudaEventRecord(c->ev_s0, st));
     RC(gs_launch_search(I, B, p->kernel, p->queue_chunk, p->ctas_per_sm, n_items, st));
     GS_CUDA(cudaEventRecord(c->ev_s1, st));
+    /* the previous chunk's results are copied out of the buffers below while
+     * this chunk searched */
+    if (co && co->wait_d2h) GS_CUDA(cudaStreamWaitEvent(st, c->ev_d2h, 0));
 
     B.rd_nf = c->rd_nf;
     B.rd_nr = c->rd_nr;
@@ -484,8 +571,8 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     RC(gs_launch_finalize_count(I, B, st));
     RC(exclusive_scan(c, c->rd_nseeds, c->seed_off, nr1));
     RC(exclusive_scan(c, c->rd_npos, c->pos_off, nr1));
-    GS_CUDA(cudaMemcpyAsync(&c->h_small[3], c->seed_off + n_reads, 8, cudaMemcpyDeviceToHost, st));
-    GS_CUDA(cudaMemcpyAsync(&c->h_small[4], c->pos_off + n_reads, 8, cudaMemcpyDeviceToHost, st));
+    RC(fetch_small(&c->h_small[3], c->seed_off + n_reads, 8, st));
+    RC(fetch_small(&c->h_small[4], c->pos_off + n_reads, 8, st));
     GS_CUDA(cudaStreamSynchronize(st));
     uint64_t n_seeds = c->h_small[3], n_pos = c->h_small[4];
     if (n_pos > 0xffffffffull * 4) {
@@ -510,6 +597,15 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
         RC(grow_host(c->h_seeds, c->cap_h_seeds, n_seeds + 1));
         RC(grow_host(c->h_pos, c->cap_h_pos, n_pos + 1));
     }
+    if (co) {
+        uint64_t ws = co->base_s + n_seeds + 1, wp = co->base_p + n_pos + 1;
+        if (co->base_s == 0 && co->base_p == 0) {
+            ws = (uint64_t)((double)ws * co->scale * 1.1);
+            wp = (uint64_t)((double)wp * co->scale * 1.1);
+        }
+        RC(grow_host_keep(c->h_seeds, c->cap_h_seeds, ws, co->base_s, c->st_copy));
+        RC(grow_host_keep(c->h_pos, c->cap_h_pos, wp, co->base_p, c->st_copy));
+    }
     RC(gs_launch_finalize_emit(I, B, st));
     if (fetch) {
         /* seeds and per-read offsets are final here: copy them out on the
@@ -525,11 +621,36 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
                                     cudaMemcpyDeviceToHost, c->st_copy));
     }
     RC(gs_launch_locate(I, B, n_seeds, n_pos, st));
+    if (co && n_reads) {
+        gs_add_base_kernel<<<152 * 4, 256, 0, st>>>(c->seed_off, c->pos_off, n_reads, co->base_s,
+                                                    co->base_p);
+        GS_CUDA(cudaGetLastError());
+    }
     GS_CUDA(cudaEventRecord(c->ev1, st));
-    GS_CUDA(cudaMemcpyAsync(&c->h_small[5], c->queue + 1, 4, cudaMemcpyDeviceToHost, st));
-    GS_CUDA(cudaMemcpyAsync(&c->h_small[10], c->queue + 2, 4, cudaMemcpyDeviceToHost, st));
-    GS_CUDA(cudaMemcpyAsync(&c->h_small[11], c->queue + 4, 4, cudaMemcpyDeviceToHost, st));
-    if (B.work) GS_CUDA(cudaMemcpyAsync(&c->h_small[6], c->d_work, 32, cudaMemcpyDeviceToHost, st));
+    RC(fetch_small(&c->h_small[5], c->queue + 1, 4, st));
+    RC(fetch_small(&c->h_small[10], c->queue + 2, 4, st));
+    RC(fetch_small(&c->h_small[11], c->queue + 4, 4, st));
+    if (B.work) RC(fetch_small(&c->h_small[6], c->d_work, 32, st));
+    if (co) {
+        /* after the small reads above: one copy engine serves both streams,
+         * and this chunk's end should not wait for its own copy-out */
+        GS_CUDA(cudaEventRecord(c->ev_done, st));
+        GS_CUDA(cudaStreamWaitEvent(c->st_copy, c->ev_done, 0));
+        GS_CUDA(cudaMemcpyAsync(c->h_seed_off + co->first_read, c->seed_off, (size_t)n_reads * 8,
+                                cudaMemcpyDeviceToHost, c->st_copy));
+        GS_CUDA(cudaMemcpyAsync(c->h_pos_off + co->first_read, c->pos_off, (size_t)n_reads * 8,
+                                cudaMemcpyDeviceToHost, c->st_copy));
+        if (n_seeds)
+            GS_CUDA(cudaMemcpyAsync(c->h_seeds + co->base_s, c->seeds,
+                                    n_seeds * sizeof(gs_seed_rec), cudaMemcpyDeviceToHost,
+                                    c->st_copy));
+        if (n_pos)
+            GS_CUDA(cudaMemcpyAsync(c->h_pos + co->base_p, c->pos, n_pos * 4,
+                                    cudaMemcpyDeviceToHost, c->st_copy));
+        GS_CUDA(cudaEventRecord(c->ev_d2h, c->st_copy));
+        co->n_seeds = n_seeds;
+        co->n_pos = n_pos;
+    }
     c->n_seeds = n_seeds;
     c->n_pos = n_pos;
     if (fetch && n_pos)
@@ -732,6 +853,89 @@ extern "C" int gs_seed_device(gs_ctx *c, const char *d_seqs, const uint64_t *d_o
     return run_pipeline(c, d_seqs, d_offsets, d_lengths, n_reads, p, fetch_to_host);
 }
 
+/* A large batch whose reads lie in order in `seqs` runs as chunks of reads:
+ * the reads go up on st_h2d chunk by chunk, each chunk is one pass on st,
+ * and its results come down on st_copy while the next chunk searches.  The
+ * host result is the batch's, as one pass would give it; the device keeps
+ * only the last chunk's, so gs_result_device and the GPU text writer do
+ * not apply (gs_result_write_text falls back to the host writer). */
+static int seed_chunked(gs_ctx *c, const char *seqs, const uint64_t *offsets, uint32_t n_reads,
+                        const gs_params *p, uint64_t bytes)
+{
+    uint32_t K = (n_reads + GS_SEED_CHUNK_READS - 1) / GS_SEED_CHUNK_READS;
+    if (K > GS_SEED_MAX_CHUNKS) K = GS_SEED_MAX_CHUNKS;
+    uint32_t first[GS_SEED_MAX_CHUNKS + 1];
+    for (uint32_t j = 0; j <= K; j++) first[j] = (uint32_t)((uint64_t)n_reads * j / K);
+    uint32_t max_n = 0;
+    for (uint32_t j = 0; j < K; j++)
+        if (first[j + 1] - first[j] > max_n) max_n = first[j + 1] - first[j];
+    /* per-read arrays the copy-out reads, sized once for every chunk */
+    RC(grow(c->seed_off, c->cap_so, (size_t)max_n + 1, c->st));
+    RC(grow(c->pos_off, c->cap_po, (size_t)max_n + 1, c->st));
+    RC(grow(c->d_seqs, c->cap_seqs, bytes + 1, c->st));
+    GS_CUDA(cudaEventRecord(c->ev_done, c->st));
+    GS_CUDA(cudaStreamWaitEvent(c->st_h2d, c->ev_done, 0));
+    for (uint32_t j = 0; j < K; j++) {
+        const uint64_t lo = offsets[first[j]];
+        const uint64_t hi = j + 1 < K ? offsets[first[j + 1]] : bytes;
+        if (hi > lo)
+            GS_CUDA(cudaMemcpyAsync(c->d_seqs + lo, seqs + lo, hi - lo, cudaMemcpyHostToDevice,
+                                    c->st_h2d));
+        GS_CUDA(cudaEventRecord(c->ev_h2d[j], c->st_h2d));
+    }
+    RC(grow_host(c->h_seed_off, c->cap_h_so, (size_t)n_reads + 1));
+    RC(grow_host(c->h_pos_off, c->cap_h_po, (size_t)n_reads + 1));
+    uint64_t bs = 0, bp = 0, walkers = 0, text_jobs = 0, work[4] = {0, 0, 0, 0};
+    float t_search = 0.f, t_total = 0.f;
+    int rc = GS_OK;
+    for (uint32_t j = 0; j < K && rc == GS_OK; j++) {
+        const uint32_t nj = first[j + 1] - first[j];
+        const cudaError_t e = cudaStreamWaitEvent(c->st, c->ev_h2d[j], 0);
+        if (e != cudaSuccess) {
+            rc = gs_cuda_fail(e, "cudaStreamWaitEvent(chunk)");
+            break;
+        }
+        GsChunkOut co;
+        memset(&co, 0, sizeof(co));
+        co.first_read = first[j];
+        co.base_s = bs;
+        co.base_p = bp;
+        co.scale = (double)n_reads / (double)(nj ? nj : 1);
+        co.wait_d2h = j > 0;
+        rc = run_pipeline(c, c->d_seqs, c->d_offsets + first[j], c->d_lengths + first[j], nj, p,
+                          0, &co);
+        if (rc) break;
+        bs += co.n_seeds;
+        bp += co.n_pos;
+        walkers += c->last_walkers;
+        text_jobs += c->last_text_jobs;
+        for (int w = 0; w < 4; w++) work[w] += c->work[w];
+        t_search += c->t_search;
+        t_total += c->t_total;
+    }
+    /* no copy may outlive the call: the caller owns the host buffers */
+    cudaStreamSynchronize(c->st_h2d);
+    cudaStreamSynchronize(c->st_copy);
+    cudaStreamSynchronize(c->st);
+    c->have_dev = 0;
+    if (rc) {
+        c->have_host = 0;
+        return rc;
+    }
+    c->h_seed_off[n_reads] = bs;
+    c->h_pos_off[n_reads] = bp;
+    c->n_reads = n_reads;
+    c->n_seeds = bs;
+    c->n_pos = bp;
+    c->last_walkers = walkers;
+    c->last_text_jobs = text_jobs;
+    memcpy(c->work, work, sizeof(work));
+    c->t_search = t_search;
+    c->t_total = t_total;
+    c->have_host = 1;
+    return GS_OK;
+}
+
 extern "C" int gs_seed(gs_ctx *c, const char *seqs, const uint64_t *offsets,
                        const uint32_t *lengths, uint32_t n_reads, const gs_params *p)
 {
@@ -751,13 +955,15 @@ extern "C" int gs_seed(gs_ctx *c, const char *seqs, const uint64_t *offsets,
                                 c->st));
         GS_CUDA(cudaMemcpyAsync(c->d_lengths, lengths, (size_t)n_reads * 4, cudaMemcpyHostToDevice,
                                 c->st));
-        GS_CUDA(cudaMemsetAsync(c->d_max, 0, 8, c->st));
+        GS_CUDA(cudaMemsetAsync(c->d_max, 0, 16, c->st));
         gs_max_end_kernel<<<(n_reads + 255) / 256, 256, 0, c->st>>>(
             c->d_offsets, c->d_lengths, n_reads, (unsigned long long *)c->d_max);
         GS_CUDA(cudaGetLastError());
-        GS_CUDA(cudaMemcpyAsync(&c->h_small[12], c->d_max, 8, cudaMemcpyDeviceToHost, c->st));
+        RC(fetch_small(&c->h_small[12], c->d_max, 16, c->st));
         GS_CUDA(cudaStreamSynchronize(c->st));
         bytes = c->h_small[12];
+        if (n_reads >= 2 * GS_SEED_CHUNK_READS && c->h_small[13] == 0)
+            return seed_chunked(c, seqs, offsets, n_reads, p, bytes);
     }
     RC(grow(c->d_seqs, c->cap_seqs, bytes + 1, c->st));
     if (bytes) GS_CUDA(cudaMemcpyAsync(c->d_seqs, seqs, bytes, cudaMemcpyHostToDevice, c->st));

@@ -169,7 +169,13 @@ int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out);
 void gs_ctx_free(gs_ctx *ctx);
 /* Reads in host memory (ASCII, one record per read, offsets in bytes):
  * copies them in, seeds, and copies the result back to host memory owned by
- * the context (valid until the next call on it). */
+ * the context (valid until the next call on it).  A batch of 2^22 reads or
+ * more whose reads lie in order in `seqs` runs as up to 16 chunks: each
+ * chunk's reads are copied in while the chunks before it run, and its
+ * results are copied out while the next one runs.  The host result is the
+ * same; the device then holds only the last chunk's, so gs_result_device
+ * and gs_result_text_device return GS_ESTATE and gs_result_write_text
+ * formats on the host. */
 int gs_seed(gs_ctx *ctx, const char *seqs, const uint64_t *offsets, const uint32_t *lengths,
             uint32_t n_reads, const gs_params *p);
 /* Reads already in device memory; fetch_to_host = 0 leaves the result on the

@@ -471,3 +471,47 @@ def test_cli_record_input(small, tmp_path):
         out = subprocess.run([gs.CLI_PATH, "-F", "-k", "19", "-s", "-o", small["prefix"],
                               str(tmp_path / name)], capture_output=True, check=True).stdout
         assert out == want.read_bytes(), name
+
+
+def _many_reads(codes, n, seed):
+    """n reads of 20-90 bases copied from the text with 1 % substitutions and
+    a few N, packed in order: (bytes, offsets, lengths)."""
+    rng = np.random.default_rng(seed)
+    lens = rng.choice(np.array([20, 33, 47, 64, 90], np.uint32), n)
+    starts = rng.integers(0, codes.size - 100, n)
+    offs = np.zeros(n, np.uint64)
+    offs[1:] = np.cumsum(lens[:-1], dtype=np.uint64)
+    total = int(lens.sum())
+    idx = np.repeat(starts - offs.astype(np.int64), lens) + np.arange(total)
+    buf = np.frombuffer(b"ACGT", np.uint8)[codes[idx]].copy()
+    sub = rng.random(total) < 0.01
+    buf[sub] = np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, int(sub.sum()))]
+    buf[rng.random(total) < 0.001] = ord("N")
+    return buf, offs, lens
+
+
+@pytest.mark.parametrize("smem", [False, True], ids=["mem", "smem"])
+def test_seed_in_chunks_matches_one_pass(small, smem):
+    """gs_seed runs a batch of 2^22 or more reads held in order as chunks,
+    copying each chunk up and its results down while the next one runs. Its
+    host result equals one device pass over the same reads, array for array.
+    A batch whose reads are not in order runs as one pass."""
+    import torch
+    ctx = small["ctx"]
+    buf, offs, lens = _many_reads(small["codes"], (1 << 22) + 123_457, seed=101 + smem)
+    got = ctx.seed(buf, offs, lens, k=19, smem=smem)
+    dev = torch.device("cuda", 0)
+    d_seqs = torch.from_numpy(buf).to(dev)
+    d_offs = torch.from_numpy(offs.view(np.int64)).to(dev)
+    d_lens = torch.from_numpy(lens.view(np.int32)).to(dev)
+    want = ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), lens.size,
+                           fetch=True, k=19, smem=smem)
+    for name in ("read_seed_off", "read_pos_off", "seeds", "pos"):
+        assert np.array_equal(getattr(got, name), getattr(want, name)), name
+    # the same reads with their order in the buffer reversed: not chunked
+    roffs = (buf.size - (offs + lens)).astype(np.uint64)
+    rbuf = np.empty_like(buf)
+    rbuf[np.repeat(roffs.astype(np.int64) - offs.astype(np.int64), lens) + np.arange(buf.size)] = buf
+    rev = ctx.seed(rbuf, roffs, lens, k=19, smem=smem)
+    for name in ("read_seed_off", "read_pos_off", "seeds", "pos"):
+        assert np.array_equal(getattr(rev, name), getattr(want, name)), name
