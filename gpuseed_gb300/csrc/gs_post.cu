@@ -32,19 +32,12 @@
 
 __device__ __forceinline__ uint32_t gs_size(const GsRec &r) { return r.u - r.l + 1u; }
 
-/* decision for forward record o of list F[0..nf) */
-__device__ __forceinline__ void gs_fwd_rule(const GsRec *F, uint32_t nf, uint32_t o, int smem,
-                                            uint32_t max_occ, bool &keep, uint32_t &cnt,
-                                            uint32_t &xl, uint32_t &xu)
+/* decision for forward record R whose next record (when has_next) is N */
+__device__ __forceinline__ void gs_fwd_rule_v(const GsRec &R, const GsRec &N, bool has_next,
+                                              int smem, uint32_t max_occ, bool &keep,
+                                              uint32_t &cnt, uint32_t &xl, uint32_t &xu)
 {
-    GsRec R = F[o];
-    bool same = false;
-    GsRec N;
-    N.l = 1; N.u = 0; N.x = 0; N.y = 0;
-    if (o + 1 < nf) {
-        N = F[o + 1];
-        same = N.x == R.x;
-    }
+    const bool same = has_next && N.x == R.x;
     uint32_t sz = gs_size(R);
     xl = 1; xu = 0;
     if (smem) {
@@ -59,19 +52,23 @@ __device__ __forceinline__ void gs_fwd_rule(const GsRec *F, uint32_t nf, uint32_
     if (max_occ && sz > max_occ) keep = false;
 }
 
-__device__ __forceinline__ void gs_rev_rule(const GsRec *Rv, uint32_t nr, uint32_t o, int smem,
+/* decision for forward record o of list F[0..nf) */
+__device__ __forceinline__ void gs_fwd_rule(const GsRec *F, uint32_t nf, uint32_t o, int smem,
                                             uint32_t max_occ, bool &keep, uint32_t &cnt,
                                             uint32_t &xl, uint32_t &xu)
 {
-    (void)nr;
-    GsRec R = Rv[o];
-    bool same = false;
-    GsRec P;
-    P.l = 1; P.u = 0; P.x = 0; P.y = 0;
-    if (o > 0) {
-        P = Rv[o - 1];
-        same = P.y == R.y;
-    }
+    GsRec N;
+    N.l = 1; N.u = 0; N.x = 0; N.y = 0;
+    if (o + 1 < nf) N = F[o + 1];
+    gs_fwd_rule_v(F[o], N, o + 1 < nf, smem, max_occ, keep, cnt, xl, xu);
+}
+
+/* decision for reverse record R whose previous record (when has_prev) is P */
+__device__ __forceinline__ void gs_rev_rule_v(const GsRec &R, const GsRec &P, bool has_prev,
+                                              int smem, uint32_t max_occ, bool &keep,
+                                              uint32_t &cnt, uint32_t &xl, uint32_t &xu)
+{
+    const bool same = has_prev && P.y == R.y;
     uint32_t sz = gs_size(R);
     xl = 1; xu = 0;
     if (smem) {
@@ -84,6 +81,17 @@ __device__ __forceinline__ void gs_rev_rule(const GsRec *Rv, uint32_t nr, uint32
         if (same) { xl = P.l; xu = P.u; }
     }
     if (max_occ && sz > max_occ) keep = false;
+}
+
+__device__ __forceinline__ void gs_rev_rule(const GsRec *Rv, uint32_t nr, uint32_t o, int smem,
+                                            uint32_t max_occ, bool &keep, uint32_t &cnt,
+                                            uint32_t &xl, uint32_t &xu)
+{
+    (void)nr;
+    GsRec P;
+    P.l = 1; P.u = 0; P.x = 0; P.y = 0;
+    if (o > 0) P = Rv[o - 1];
+    gs_rev_rule_v(Rv[o], P, o > 0, smem, max_occ, keep, cnt, xl, xu);
 }
 
 /* Compacts the records among slots s0..s0+n (flagged in the record mask;
@@ -145,13 +153,17 @@ __device__ __forceinline__ uint32_t gs_warp_compact(GsRec *slots, const uint32_t
  * round: forward records (slots s0..s0+n) go to s0 + rank, reverse ones
  * (s0+n..s0+2n) to s0 + n + rank -- one round of mask words, one of
  * records, for both.  Every target is at or before its source and earlier
- * records' targets lie before later records' sources, so in place is safe. */
+ * records' targets lie before later records' sources, so in place is safe.
+ * mine: lane j's record among the first 32 (forward, then reverse). */
 __device__ __forceinline__ void gs_warp_compact_both(GsRec *slots, const uint32_t *mask, uint64_t s0,
                                                      uint32_t n, int lane, uint32_t &nf,
-                                                     uint32_t &nr)
+                                                     uint32_t &nr, GsRec &mine)
 {
     const uint64_t s1 = s0 + n, s2 = s0 + 2ull * n;
     const uint64_t w0 = s0 >> 5, wend = (s2 + 31) >> 5;   /* at most 32 words */
+    mine.x = mine.y = 0;
+    mine.l = 1u;
+    mine.u = 0u;
     const uint64_t w = w0 + (uint64_t)lane;
     uint32_t mf = 0, mr = 0;
     if (w < wend) {
@@ -196,11 +208,15 @@ __device__ __forceinline__ void gs_warp_compact_both(GsRec *slots, const uint32_
         const uint32_t bf = __shfl_sync(0xffffffffu, incf - cf, L);
         const uint32_t br = __shfl_sync(0xffffffffu, incr - cr, L);
         GsRec rec;
+        rec.x = rec.y = 0;
+        rec.l = 1u;
+        rec.u = 0u;
         if (v) {
             const uint32_t word = rev ? wr : wf;
             const uint32_t bit = __fns(word, 0, (int)(jj - (rev ? br : bf)) + 1);
             rec = slots[((w0 + (uint64_t)L) << 5) + bit];
         }
+        if (g == 0) mine = rec;
         __syncwarp();
         if (v) slots[(rev ? s1 : s0) + jj] = rec;
         __syncwarp();
@@ -212,9 +228,19 @@ __global__ void __launch_bounds__(256) gs_finalize_count(GsBatch B)
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    uint64_t so0 = 0, so1 = 0;
+    if (warp < B.n_reads) {
+        so0 = B.slot_off[warp];
+        so1 = B.slot_off[warp + 1];
+    }
     for (uint32_t r = warp; r < B.n_reads; r += nwarps) {
-        uint64_t base = B.slot_off[r];
-        if (B.slot_off[r + 1] > B.slot_cap) {
+        const uint64_t base = so0, next = so1;
+        /* the next read's slot range, loaded while this one is compacted */
+        if (r + nwarps < B.n_reads) {
+            so0 = B.slot_off[r + nwarps];
+            so1 = B.slot_off[r + nwarps + 1];
+        }
+        if (next > B.slot_cap) {
             /* a replayed pass whose input needs more slots than it was sized
              * for: nothing of this read is there; the host re-sizes */
             if (lane == 0) {
@@ -226,23 +252,50 @@ __global__ void __launch_bounds__(256) gs_finalize_count(GsBatch B)
             }
             continue;
         }
-        uint32_t n = (uint32_t)((B.slot_off[r + 1] - base) >> 1);
+        uint32_t n = (uint32_t)((next - base) >> 1);
         GsRec *F = B.slots + base;
         GsRec *Rv = F + n;
         uint32_t nf, nr;
+        uint64_t seeds = 0, npos = 0;
+        bool done = false;
         if (2u * n + 31u <= 1024u) {
-            gs_warp_compact_both(B.slots, B.recmask, base, n, lane, nf, nr);
+            GsRec mine;
+            gs_warp_compact_both(B.slots, B.recmask, base, n, lane, nf, nr, mine);
+            if (nf + nr <= 32u) {
+                /* lane j holds record j of [forward | reverse]: the rules'
+                 * neighbours are lanes j+1 (forward) and j-1 (reverse) */
+                GsRec up, dn;
+                up.x = __shfl_down_sync(0xffffffffu, mine.x, 1);
+                up.y = __shfl_down_sync(0xffffffffu, mine.y, 1);
+                up.l = __shfl_down_sync(0xffffffffu, mine.l, 1);
+                up.u = __shfl_down_sync(0xffffffffu, mine.u, 1);
+                dn.x = __shfl_up_sync(0xffffffffu, mine.x, 1);
+                dn.y = __shfl_up_sync(0xffffffffu, mine.y, 1);
+                dn.l = __shfl_up_sync(0xffffffffu, mine.l, 1);
+                dn.u = __shfl_up_sync(0xffffffffu, mine.u, 1);
+                const uint32_t j = (uint32_t)lane;
+                bool keep = false;
+                uint32_t cnt = 0, xl, xu;
+                if (j < nf)
+                    gs_fwd_rule_v(mine, up, j + 1 < nf, B.smem, B.max_occ, keep, cnt, xl, xu);
+                else if (j < nf + nr)
+                    gs_rev_rule_v(mine, dn, j > nf, B.smem, B.max_occ, keep, cnt, xl, xu);
+                if (keep && cnt) {
+                    seeds = 1;
+                    npos = cnt;
+                }
+                done = true;
+            }
         } else {
             nf = gs_warp_compact(B.slots, B.recmask, base, n, lane);
             nr = gs_warp_compact(B.slots, B.recmask, base + n, n, lane);
         }
-        uint64_t seeds = 0, npos = 0;
-        for (uint32_t o = lane; o < nf; o += 32) {
+        for (uint32_t o = lane; !done && o < nf; o += 32) {
             bool keep; uint32_t cnt, xl, xu;
             gs_fwd_rule(F, nf, o, B.smem, B.max_occ, keep, cnt, xl, xu);
             if (keep && cnt) { seeds++; npos += cnt; }
         }
-        for (uint32_t o = lane; o < nr; o += 32) {
+        for (uint32_t o = lane; !done && o < nr; o += 32) {
             bool keep; uint32_t cnt, xl, xu;
             gs_rev_rule(Rv, nr, o, B.smem, B.max_occ, keep, cnt, xl, xu);
             if (keep && cnt) { seeds++; npos += cnt; }
