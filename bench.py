@@ -372,6 +372,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-text", action="store_true")
+    ap.add_argument("--no-text-index", action="store_true",
+                    help="seed without the full-SA / text structures")
     ap.add_argument("--serve-batch", type=int, default=1 << 20,
                     help="serving: most reads merged into one pass")
     ap.add_argument("--retune", action="store_true")
@@ -392,6 +394,10 @@ def main():
 
     w = workload(args.config, args.ref_len, args.reads, rank=rank)
     idx = w["idx"]
+    if not args.no_text_index:
+        t0 = time.time()
+        idx.set_text(4)
+        log(f"[bench] text structures (full SA, text, ISA samples) built in {time.time() - t0:.2f}s")
     seqs, offs, lens = w["seqs"], w["offs"], w["lens"]
     n_reads = int(lens.size)
     k, smem = w["k"], w["smem"]

@@ -31,7 +31,6 @@ struct gs_index {
 extern "C" int gs_index_set_kmer_len(gs_index *idx, int kx);
 extern "C" int gs_index_set_text(gs_index *idx, int min_steps);
 
-#define GS_TEXT_MIN_DEFAULT 4
 #define GS_SAF_UNSET 0xfffffffeu
 #define GS_CHAIN_MAX (1u << 20)   /* LF steps one chain may take */
 
@@ -258,12 +257,9 @@ static int upload(uint32_t primary, const uint32_t L2_1to4[4], const uint32_t *b
         gs_index_free(idx);
         return rc;
     }
-    /* the longer table and the text structures are accelerators: without
-     * room for them, run without */
+    /* the longer table is an accelerator: without room for it, run without */
     for (int kx = auto_kmer_len(seq_len); kx > GS_K0; kx--)
         if (gs_index_set_kmer_len(idx, kx) == GS_OK) break;
-    cudaGetLastError();
-    (void)gs_index_set_text(idx, GS_TEXT_MIN_DEFAULT);
     cudaGetLastError();
     *out = idx;
     return GS_OK;

@@ -138,9 +138,12 @@ int gs_index_build(const uint8_t *codes, uint64_t n, uint32_t sa_intv, int devic
  * not change; seeding uses it only when k > len. */
 int gs_index_set_kmer_len(gs_index *idx, int kmer_len);
 /* Text structures in HBM, built from the .bwt and .sa by one pass of LF
- * chains (4 * seq_len bytes of full suffix array, seq_len / 4 of packed text,
- * seq_len of inverse-SA samples every 4 positions; loading builds them when
- * the memory is there, with min_steps 4).  With them, locate reads each
+ * chains: 4 * seq_len bytes of full suffix array, seq_len / 4 of packed
+ * text, seq_len of inverse-SA samples every 4 positions (16.3 GB and
+ * 0.3-0.5 s at 3.1 Gbp).  Loading does not build them: on config-3 reads
+ * they save ~1.6 ms per million reads, so they pay for their build after a
+ * few hundred million reads.  min_steps 4 is the measured best.  With them,
+ * locate reads each
  * position from the full suffix array instead of walking to a sampled row,
  * and a walker whose interval has been one row, with its containment test
  * over, for min_steps steps (so that the row is the read's own locus, not a

@@ -22,6 +22,7 @@ def _gpu_index(tmp, codes, name):
     import gpuseed_gb300 as gs
     prefix = os.path.join(str(tmp), name)
     idx = gs.build_index(codes, 7, prefix=prefix)
+    idx.set_text(4)         # full SA, text and ISA samples: locate and text mode use them
     return prefix, idx
 
 

@@ -37,6 +37,7 @@ def small(built, tmp_path_factory):
     prefix = build_index(d, codes, sa_intv=7)
     gs = _gs()
     gidx = gs.Index(prefix)
+    gidx.set_text(4)        # the text structures are built on request
     oidx = pyoracle.Index(prefix)
     ctx = gs.Context(gidx)
     return dict(codes=codes, prefix=prefix, gidx=gidx, oidx=oidx, ctx=ctx, dir=d)
@@ -174,8 +175,9 @@ def test_text_mode(small, text_min):
 
 
 def test_text_build_checks_samples(small):
-    """An .sa whose samples do not continue the BWT's chains gets no text
-    structures (GS_EFORMAT); the index still loads and seeds by LF walks."""
+    """Building the text structures for an .sa whose samples do not continue
+    the BWT's chains fails with GS_EFORMAT and leaves the index seeding by LF
+    walks; the consistent files build them."""
     gs = _gs()
     prefix = small["prefix"]
     bwt = np.fromfile(prefix + ".bwt", dtype=np.uint32)
@@ -188,7 +190,9 @@ def test_text_build_checks_samples(small):
         gidx.set_text(24)
     assert e.value.code == -3        # GS_EFORMAT
     ok = gs.Index(arrays=(int(bwt[0]), bwt[1:5], bwt[5:], sa[7:], int(sa[5])))
-    assert ok.info().text_min > 0
+    assert ok.info().text_min == 0      # not built at load
+    ok.set_text(4)
+    assert ok.info().text_min == 4
 
 
 def test_empty_batch(small):
@@ -244,8 +248,9 @@ def test_cli_matches_oracle(small, tmp_path):
         opath = tmp_path / "o.txt"
         ob.write_text(str(opath), 1, smem)
         # default batch, and batches of one read, ~10 reads, ~70 reads (the
-        # reader thread parses the next batch while one is seeded)
-        for batch in ([], ["-B", "1"], ["-B", "1000"], ["-B", "7000"]):
+        # reader thread parses the next batch while one is seeded), with and
+        # without the text structures (-T)
+        for batch in ([], ["-B", "1"], ["-B", "1000"], ["-B", "7000"], ["-T"], ["-T", "-B", "1000"]):
             args = ([gs.CLI_PATH, "-k", "19"] + (["-s"] if smem else []) + batch +
                     ["-o", small["prefix"], str(fa)])
             out = subprocess.run(args, capture_output=True, check=True).stdout
