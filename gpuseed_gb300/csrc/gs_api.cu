@@ -862,10 +862,15 @@ extern "C" int gs_seed_device(gs_ctx *c, const char *d_seqs, const uint64_t *d_o
 static int seed_chunked(gs_ctx *c, const char *seqs, const uint64_t *offsets, uint32_t n_reads,
                         const gs_params *p, uint64_t bytes)
 {
-    uint32_t K = (n_reads + GS_SEED_CHUNK_READS - 1) / GS_SEED_CHUNK_READS;
+    /* the first and the last chunk are half-size: the first one's copy-in
+     * and the last one's copy-out are the only copies nothing overlaps */
+    uint32_t K = (n_reads + GS_SEED_CHUNK_READS - 1) / GS_SEED_CHUNK_READS + 1;
     if (K > GS_SEED_MAX_CHUNKS) K = GS_SEED_MAX_CHUNKS;
     uint32_t first[GS_SEED_MAX_CHUNKS + 1];
-    for (uint32_t j = 0; j <= K; j++) first[j] = (uint32_t)((uint64_t)n_reads * j / K);
+    first[0] = 0;
+    for (uint32_t j = 1; j < K; j++)
+        first[j] = (uint32_t)((uint64_t)n_reads * (2 * j - 1) / (2 * (K - 1)));
+    first[K] = n_reads;
     uint32_t max_n = 0;
     for (uint32_t j = 0; j < K; j++)
         if (first[j + 1] - first[j] > max_n) max_n = first[j + 1] - first[j];

@@ -478,6 +478,28 @@ def test_cli_record_input(small, tmp_path):
         assert out == want.read_bytes(), name
 
 
+def _text_digest(ctx, smem):
+    """SHA-1 of the context's -o records, streamed through a pipe."""
+    import hashlib
+    import threading
+    rfd, wfd = os.pipe()
+    h = hashlib.sha1()
+
+    def drain():
+        with os.fdopen(rfd, "rb") as f:
+            for block in iter(lambda: f.read(1 << 20), b""):
+                h.update(block)
+
+    t = threading.Thread(target=drain)
+    t.start()
+    try:
+        ctx.write_text(wfd, 1, smem)
+    finally:
+        os.close(wfd)
+        t.join()
+    return h.hexdigest()
+
+
 def _many_reads(codes, n, seed):
     """n reads of 20-90 bases copied from the text with 1 % substitutions and
     a few N, packed in order: (bytes, offsets, lengths)."""
@@ -505,6 +527,7 @@ def test_seed_in_chunks_matches_one_pass(small, smem):
     ctx = small["ctx"]
     buf, offs, lens = _many_reads(small["codes"], (1 << 22) + 123_457, seed=101 + smem)
     got = ctx.seed(buf, offs, lens, k=19, smem=smem)
+    got_text = _text_digest(ctx, smem)      # formatted by the host: no device result
     dev = torch.device("cuda", 0)
     d_seqs = torch.from_numpy(buf).to(dev)
     d_offs = torch.from_numpy(offs.view(np.int64)).to(dev)
@@ -513,6 +536,7 @@ def test_seed_in_chunks_matches_one_pass(small, smem):
                            fetch=True, k=19, smem=smem)
     for name in ("read_seed_off", "read_pos_off", "seeds", "pos"):
         assert np.array_equal(getattr(got, name), getattr(want, name)), name
+    assert got_text == _text_digest(ctx, smem)   # the device pass's, formatted on the GPU
     # the same reads with their order in the buffer reversed: not chunked
     roffs = (buf.size - (offs + lens)).astype(np.uint64)
     rbuf = np.empty_like(buf)
