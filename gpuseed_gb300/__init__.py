@@ -188,7 +188,7 @@ class Index:
     def text_table(self, which: int) -> np.ndarray:
         """Full SA (0), packed text words (1) or inverse-SA samples (2)."""
         info = self.info()
-        n = {0: info.seq_len + 1, 1: (info.seq_len + 15) // 16, 2: info.seq_len // 4 + 1}[which]
+        n = {0: info.seq_len + 1, 1: (info.seq_len + 15) // 16, 2: info.seq_len // 2 + 1}[which]
         out = np.empty(n, dtype=np.uint32)
         check(lib().gs_index_text_table(self.h, which, 0, n, _ptr(out)))
         return out

@@ -37,7 +37,7 @@
  * text_min: a walker that has taken this many steps with a one-row interval
  *       and no neighbour interval, with 16 or more bases left, compares the
  *       read with the text (0: never). */
-#define GS_ISA_STEP 4u
+#define GS_ISA_STEP 2u
 #define GS_TEXT_MARK 0xf0000000u     /* jl of a text-mode walker */
 #define GS_REGIME_MARK 0xe0000000u   /* jl (+ steps) of a one-row walker without J */
 struct GsDevIndex {

@@ -139,7 +139,7 @@ int gs_index_build(const uint8_t *codes, uint64_t n, uint32_t sa_intv, int devic
 int gs_index_set_kmer_len(gs_index *idx, int kmer_len);
 /* Text structures in HBM, built from the .bwt and .sa by one pass of LF
  * chains: 4 * seq_len bytes of full suffix array, seq_len / 4 of packed
- * text, seq_len of inverse-SA samples every 4 positions (16.3 GB and
+ * text, 2 * seq_len of inverse-SA samples every 2 positions (19.4 GB and
  * 0.3-0.5 s at 3.1 Gbp).  Loading does not build them: on config-3 reads
  * they save ~1.6 ms per million reads, so they pay for their build after a
  * few hundred million reads.  min_steps 4 is the measured best.  With them,
@@ -155,7 +155,7 @@ int gs_index_set_kmer_len(gs_index *idx, int kmer_len);
 int gs_index_set_text(gs_index *idx, int min_steps);
 /* Copies entries [first, first+count) of a text structure to host memory:
  * which 0 = full suffix array (seq_len+1 rows), 1 = packed text words
- * (ceil(seq_len/16)), 2 = inverse-SA samples (seq_len/4 + 1). */
+ * (ceil(seq_len/16)), 2 = inverse-SA samples (seq_len/2 + 1). */
 int gs_index_text_table(const gs_index *idx, int which, uint64_t first, uint64_t count,
                         uint32_t *out);
 /* Keeps the occurrence table in L2 under an access-policy window on the

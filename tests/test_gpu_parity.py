@@ -122,7 +122,7 @@ def test_text_structures(small):
     assert np.array_equal(gidx.text_table(1), words.astype(np.uint32))
     isa = np.empty(n + 1, np.int64)
     isa[sa.astype(np.int64)] = np.arange(n + 1)
-    assert np.array_equal(gidx.text_table(2), isa[::4].astype(np.uint32))
+    assert np.array_equal(gidx.text_table(2), isa[::2].astype(np.uint32))
 
 
 def text_mode_reads(small):
