@@ -558,6 +558,59 @@ __global__ void __launch_bounds__(256, 5) gs_search_lockstep(GsDevIndex I, GsBat
 #define GS_TM_MOVED (1u << 25)   /* the compare advanced past the entry position */
 #define GS_TM_CONT (1u << 24)    /* a wildcard base follows: back to the interval walk */
 
+/* The 2-bit codes (forward or complement table) and the non-ACGT flags of 4
+ * ASCII bytes: a byte-permute lookup of the nibble table, indexed by ch & 7 */
+__device__ __forceinline__ void gs_codes4(uint32_t b, bool fwd, uint32_t &packed, uint32_t &inv)
+{
+    const uint32_t idx = b & 0x07070707u;
+    const uint32_t sel = (idx & 7u) | ((idx >> 4) & 0x70u) | ((idx >> 8) & 0x700u) |
+                         ((idx >> 12) & 0x7000u);
+    /* bytes 0..7 = code of ch & 7: forward A0 C1 G2 T3 N4 others 0/5, complement */
+    const uint32_t c = fwd ? __byte_perm(0x01000005u, 0x02040003u, sel)
+                           : __byte_perm(0x02000305u, 0x01040000u, sel);
+    uint32_t v = c & 0x03030303u;
+    v = (v | (v >> 6)) & 0x000f000fu;
+    packed = (v | (v >> 12)) & 0xffu;
+    uint32_t iv = (c >> 2) & 0x01010101u;   /* codes 4 and 5 */
+    iv = (iv | (iv >> 7)) & 0x00030003u;
+    inv = (iv | (iv >> 14)) & 0xfu;
+}
+
+/* The read's next `avail` (1..16) bases in walk order from pos: the first at
+ * bits 30-31 of *wr (2-bit codes), and *inv with bit 31 - i set when the
+ * i-th is not ACGT.  Loads the aligned words that hold the bytes, each of
+ * which holds at least one byte of the read. */
+__device__ __forceinline__ void gs_read_window(const unsigned char *seq, int pos, bool fwd,
+                                               int avail, uint32_t &wr, uint32_t &inv32)
+{
+    const unsigned char *lo = seq + (fwd ? pos - avail : pos + 1);
+    const uintptr_t a = (uintptr_t)lo;
+    const uint32_t *wp = (const uint32_t *)(a & ~(uintptr_t)3);
+    const uint32_t off = (uint32_t)(a & 3u);
+    const uint32_t nw = (off + (uint32_t)avail + 3u) >> 2;   /* 1..5 */
+    uint32_t w[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++) w[k] = (uint32_t)k < nw ? __ldg(wp + k) : 0u;
+    uint32_t wr16 = 0, inv16 = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        uint32_t p, iv;
+        gs_codes4(__funnelshift_r(w[k], w[k + 1], off * 8u), fwd, p, iv);
+        wr16 |= p << (8 * k);
+        inv16 |= iv << (4 * k);
+    }
+    if (fwd) {
+        /* memory order ends with the first base of the walk (pos-1) */
+        wr = wr16 << (2 * (16 - avail));
+        inv32 = inv16 << (32 - avail);
+    } else {
+        /* memory order starts with it (pos+1): reverse the 2-bit groups */
+        uint32_t x = __brev(wr16);
+        wr = ((x >> 1) & 0x55555555u) | ((x & 0x55555555u) << 1);
+        inv32 = __brev(inv16) & (0xffffffffu << (32 - avail));
+    }
+}
+
 template <int COUNT>
 __device__ __forceinline__ bool gs_text_round(const GsDevIndex &I, const unsigned char *seq, int iL,
                                               bool fwd, int dir, uint32_t &l, uint32_t &u,
@@ -589,14 +642,9 @@ __device__ __forceinline__ bool gs_text_round(const GsDevIndex &I, const unsigne
                 wt = __ldg(&I.text[0]) << ((16u - q) << 1);
             }
             /* the read's next bases in walk order, the first at bits 30-31 */
-            uint32_t wr = 0;
-#pragma unroll 1
-            for (int i = 0; i < avail; i++) {
-                const unsigned char ch = seq[pos + dir * (i + 1)];
-                const uint32_t c = fwd ? gs_fwd_code(ch) : gs_comp_code(ch);
-                if (c > 3u && bad == avail) bad = i;
-                wr |= (c & 3u) << (30 - 2 * i);
-            }
+            uint32_t wr, inv32;
+            gs_read_window(seq, pos, fwd, avail, wr, inv32);
+            if (inv32) bad = __clz(inv32);
             m = (int)(__clz(wr ^ wt) >> 1);
             if (m > bad) m = bad;
             pos += dir * m;
