@@ -16,6 +16,7 @@ def env(built, tmp_path_factory):
     codes = random_reference(200_000, 77, dups=40)
     prefix = build_index(tmp_path_factory.mktemp("srv"), codes, sa_intv=7)
     idx = gs.Index(prefix)
+    idx.set_text(4)     # a resident server would build them: passes use text mode
     return dict(codes=codes, idx=idx, ctx=gs.Context(idx))
 
 

@@ -19,7 +19,10 @@ from helpers import build_index, pack, random_reference, sample_reads
 pytestmark = pytest.mark.gpu
 
 
-def test_noalloc_matches_allocating_entry_point(built, tmp_path):
+@pytest.mark.parametrize("text", [False, True], ids=["lf_walk", "full_sa"])
+def test_noalloc_matches_allocating_entry_point(built, tmp_path, text):
+    """text: the index holds the full suffix array, so both entry points
+    locate by one read of it instead of walking to a sampled row."""
     import torch
 
     import gpuseed_gb300 as gs
@@ -27,6 +30,8 @@ def test_noalloc_matches_allocating_entry_point(built, tmp_path):
     codes = random_reference(120_000, 31, dups=30)
     prefix = build_index(tmp_path, codes, sa_intv=7)
     idx = gs.Index(prefix)
+    if text:
+        idx.set_text(4)
     ctx = gs.Context(idx)
     dev = torch.device("cuda", 0)
     batches = [sample_reads(codes, 700, seed=41, lengths=(50, 100, 150, 250), err=0.02),
