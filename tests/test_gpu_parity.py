@@ -104,9 +104,9 @@ def test_edge_cases(small):
 
 
 def test_text_structures(small):
-    """The full suffix array, packed text and inverse-SA samples that loading
-    builds in HBM from the .bwt and .sa equal the oracle's suffix array and
-    the text."""
+    """The full suffix array, packed text and inverse-SA samples that
+    gs_index_set_text builds in HBM from the .bwt and .sa equal the oracle's
+    suffix array and the text."""
     gidx = small["gidx"]
     assert gidx.info().text_min > 0
     codes = small["codes"]
