@@ -544,3 +544,30 @@ def test_seed_in_chunks_matches_one_pass(small, smem):
     rev = ctx.seed(rbuf, roffs, lens, k=19, smem=smem)
     for name in ("read_seed_off", "read_pos_off", "seeds", "pos"):
         assert np.array_equal(getattr(rev, name), getattr(want, name)), name
+
+
+def test_graph_recaptures_after_index_change(small):
+    """A pass captured into a CUDA graph holds the index's device pointers;
+    freeing or rebuilding the text structures or the start table bumps the
+    index's generation, so the next call captures again instead of replaying
+    with freed buffers.  Every call gives the oracle's seeds."""
+    import torch
+    gs = _gs()
+    gidx = gs.Index(small["prefix"])
+    gidx.set_text(4)
+    ctx = gs.Context(gidx)
+    reads = sample_reads(small["codes"], 300, seed=131, lengths=(60, 120, 250), err=0.01)
+    seqs, offs, lens = pack(reads)
+    dev = torch.device("cuda", 0)
+    d_seqs = torch.from_numpy(np.frombuffer(seqs, np.uint8).copy()).to(dev)
+    d_offs = torch.from_numpy(offs.view(np.int64)).to(dev)
+    d_lens = torch.from_numpy(lens.view(np.int32)).to(dev)
+    ob = small["oidx"].seed(seqs, offs, lens, k=19, smem=True)
+    changes = [lambda: None, lambda: gidx.set_text(0), lambda: gidx.set_text(4),
+               lambda: gidx.set_text(-1), lambda: gidx.set_kmer_len(14), lambda: gidx.set_text(2)]
+    for step, change in enumerate(changes):
+        change()
+        for rep in range(2):     # capture (or replay), then replay
+            gres = ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(),
+                                   lens.size, fetch=True, k=19, smem=True, graph=True)
+            assert_same(gres, ob, lens.size, f"change {step} rep {rep}")
