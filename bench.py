@@ -217,7 +217,7 @@ def cpu_baseline(prefix, seqs, offs, lens, k, smem, table, target_s=12.0, thread
 # --------------------------------------------------------------------------
 # serving: Poisson arrivals of config-5 requests against the resident index
 
-def serving_sweep(idx, codes, nmask, k, smem, peak_reads_s, max_batch_reads=1 << 20, n_slots=4,
+def serving_sweep(idx, codes, nmask, k, smem, peak_reads_s, max_batch_reads=1 << 18, n_slots=12,
                   loads=(0.1, 0.5, 0.9, 1.2), modes=("continuous", "per_request"),
                   seconds=1.5, seed=0x5EED1005):
     import gpuseed_gb300 as gs
@@ -374,7 +374,8 @@ def main():
     ap.add_argument("--no-text", action="store_true")
     ap.add_argument("--no-text-index", action="store_true",
                     help="seed without the full-SA / text structures")
-    ap.add_argument("--serve-batch", type=int, default=1 << 20,
+    ap.add_argument("--serve-slots", type=int, default=12)
+    ap.add_argument("--serve-batch", type=int, default=1 << 18,
                     help="serving: most reads merged into one pass")
     ap.add_argument("--retune", action="store_true")
     args = ap.parse_args()
@@ -602,7 +603,7 @@ def main():
     latency = None
     if rank == 0 and not args.no_serving:
         latency = serving_sweep(idx, w["codes"], w["nmask"], k, smem, value / ws,
-                                max_batch_reads=args.serve_batch)
+                                max_batch_reads=args.serve_batch, n_slots=args.serve_slots)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -365,7 +365,7 @@ class Context:
 class Server:
     """Serving loop: resident index, requests merged into passes as slots free up."""
 
-    def __init__(self, index: Index, n_slots=4, max_batch_reads=0, hbm_budget=0, **params):
+    def __init__(self, index: Index, n_slots=0, max_batch_reads=0, hbm_budget=0, **params):
         self.index = index
         o = ServerOpts(n_slots, max_batch_reads, hbm_budget, Context.params(**params))
         h = C.c_void_p()

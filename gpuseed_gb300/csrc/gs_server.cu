@@ -245,9 +245,9 @@ extern "C" int gs_server_start(gs_index *idx, const gs_server_opts *opts, gs_ser
     gs_server *s = new gs_server();
     s->idx = idx;
     s->opts = *opts;
-    if (s->opts.n_slots <= 0) s->opts.n_slots = 4;
+    if (s->opts.n_slots <= 0) s->opts.n_slots = 12;
     if (s->opts.n_slots > 64) s->opts.n_slots = 64;
-    if (s->opts.max_batch_reads <= 0) s->opts.max_batch_reads = 1 << 20;
+    if (s->opts.max_batch_reads <= 0) s->opts.max_batch_reads = 1 << 18;
     s->stopping = false;
     s->next_id = 1;
     s->reserved = 0;
