@@ -9,9 +9,11 @@
  * code and never exits; gs_last_error() describes the last failure of the
  * calling thread.
  *
- * Threading: a gs_index is immutable after loading and may be shared by
- * threads; a gs_ctx (stream + workspace + last result) belongs to one host
- * thread at a time.
+ * Threading: a gs_index may be shared by threads; it changes only through
+ * gs_index_set_kmer_len / _set_text / _set_l2_window, which must not overlap
+ * a pass on any of its contexts (a context's captured pass is captured
+ * again after such a change).  A gs_ctx (stream + workspace + last result)
+ * belongs to one host thread at a time.
  */
 #ifndef GPUSEED_H
 #define GPUSEED_H
@@ -135,7 +137,8 @@ int gs_index_build(const uint8_t *codes, uint64_t n, uint32_t sa_intv, int devic
  * lower length is taken when the memory is not there).  A candidate starts
  * from the interval of its first len bases instead of 13 + len-13 steps: the
  * SA interval of a string does not depend on how it is found, so results do
- * not change; seeding uses it only when k > len. */
+ * not change; seeding uses it only when k > len.  Call while no pass runs on
+ * a context of this index. */
 int gs_index_set_kmer_len(gs_index *idx, int kmer_len);
 /* Text structures in HBM, built from the .bwt and .sa by one pass of LF
  * chains: 4 * seq_len bytes of full suffix array, seq_len / 4 of packed
