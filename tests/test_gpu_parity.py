@@ -571,3 +571,41 @@ def test_graph_recaptures_after_index_change(small):
             gres = ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(),
                                    lens.size, fetch=True, k=19, smem=True, graph=True)
             assert_same(gres, ob, lens.size, f"change {step} rep {rep}")
+
+
+@pytest.mark.parametrize("n", [50_001, 49_999, 65_537], ids=["odd", "odd2", "pow2+1"])
+def test_text_structures_odd_lengths(built, tmp_path, n):
+    """References whose length is odd and not a multiple of 16: the packed
+    text ends in a partial word and the text end has no inverse-SA sample
+    (its row is row 0).  Reads at both ends of the text walk there in text
+    mode (entered after one step); every kernel and mode gives the oracle's
+    seeds, and the structures equal the oracle's suffix array and text."""
+    gs = _gs()
+    codes = random_reference(n, 500 + n % 97)
+    prefix = build_index(tmp_path, codes, sa_intv=7)
+    gidx = gs.Index(prefix)
+    gidx.set_text(1)
+    oidx = pyoracle.Index(prefix)
+    sa = pyoracle.suffix_array(codes)
+    want = sa.copy()
+    want[0] = 0xffffffff
+    assert np.array_equal(gidx.text_table(0), want)
+    isa = np.empty(n + 1, np.int64)
+    isa[sa.astype(np.int64)] = np.arange(n + 1)
+    assert np.array_equal(gidx.text_table(2), isa[::2].astype(np.uint32))
+    text = "".join("ACGT"[c] for c in codes)
+    reads = []
+    for L in (19, 20, 33, 64, 130, 250):
+        reads += [text[:L].encode(), text[n - L:].encode(), text[n - L - 7:n - 7].encode()]
+        j = L // 2
+        s = text[n - L:]
+        reads.append((s[:j] + "ACGT"[("ACGT".index(s[j]) + 2) % 4] + s[j + 1:]).encode())
+    reads += sample_reads(codes, 150, seed=n, lengths=(20, 64, 150, 250), err=0.01)
+    seqs, offs, lens = pack(reads)
+    ctx = gs.Context(gidx)
+    for kernel in (0, 1, 2):
+        for smem in (False, True):
+            for n_mode in (0, 1):
+                gres = ctx.seed(seqs, offs, lens, k=19, smem=smem, n_mode=n_mode, kernel=kernel)
+                ob = oidx.seed(seqs, offs, lens, k=19, smem=smem, n_mode=n_mode)
+                assert_same(gres, ob, len(reads), f"n={n} kernel={kernel} smem={smem} N={n_mode}")
