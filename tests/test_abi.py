@@ -80,3 +80,33 @@ def test_null_arguments(built):
     assert L.gs_seed(None, None, None, None, 0, None) == -1
     assert L.gs_index_load(None, 0, None) == -1
     assert L.gs_result_host(None, None) == -1
+
+
+def test_python_structs_match_the_header(built, tmp_path):
+    """Every ctypes mirror of a header struct has the C size and field offsets
+    (gcc on include/gpuseed.h prints them)."""
+    import subprocess
+    import gpuseed_gb300 as gs
+    mirrors = {"gs_params": gs.Params, "gs_seed_rec": gs.SeedRec, "gs_result_view": gs.ResultView,
+               "gs_index_info": gs.IndexInfo, "gs_server_opts": gs.ServerOpts,
+               "gs_server_stats": gs.ServerStats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gpuseed.h"', 'int main(void) {']
+    for cname, py in mirrors.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, check=True, text=True).stdout
+    got = {}
+    for line in out.splitlines():
+        cname, field, value = line.split()
+        got[(cname, field)] = int(value)
+    for cname, py in mirrors.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
