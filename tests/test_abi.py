@@ -80,6 +80,10 @@ def test_null_arguments(built):
     assert L.gs_seed(None, None, None, None, 0, None) == -1
     assert L.gs_index_load(None, 0, None) == -1
     assert L.gs_result_host(None, None) == -1
+    assert L.gs_index_set_text(None, 4) == -1
+    assert L.gs_index_text_table(None, 0, 0, 0, None) == -1
+    assert L.gs_ctx_last_text_jobs(None, None, None) == -1
+    assert L.gs_ctx_last_walkers(None, None, None) == -1
 
 
 def test_python_structs_match_the_header(built, tmp_path):
