@@ -203,9 +203,12 @@ static void seg_sort(const uint64_t *kin, uint64_t *kout, const V *vin, V *vout,
 #define BASE_BATCH_SIZE 1000000
 #define OUTPUT_SIZE_MUL 3
 
+/* n_fwd_out (may be NULL): per read, the forward records the reference's
+ * search kept after its own pruning (n_smems_fow), the count its MEM filter
+ * branches on (seed_gen.cu:1110-1113) */
 extern "C" int ref_run(const char *prefix, const char *seqs, const uint64_t *offs,
                        const uint32_t *lens, uint32_t n_reads, int min_seed_size, int is_smem,
-                       const char *out_path)
+                       const char *out_path, uint32_t *n_fwd_out)
 {
     bwt_t bwt;
     int pre_calc_seed_len = 13;
@@ -317,6 +320,7 @@ extern "C" int ref_run(const char *prefix, const char *seqs, const uint64_t *off
                                     bwt, pre_calc_seed_len, n_seed_cands);
         });
         for (int r = 0; r < total_reads; r++) {
+            if (n_fwd_out) n_fwd_out[reads_processed + r] = n_smems_fow[r];
             n_smems_max_gpu[0] = std::max(n_smems_max_gpu[0], n_smems_fow[r]);
             n_smems_max_gpu[1] = std::max(n_smems_max_gpu[1], n_smems_rev[r]);
         }
