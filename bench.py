@@ -190,6 +190,10 @@ def sum_over_ranks(dist, value, device=None):
 # CPU baseline (oracle port, all host threads, bounded sample)
 
 def cpu_baseline(prefix, seqs, offs, lens, k, smem, table, target_s=12.0, threads=0):
+    """The oracle's containment-stopped walk (the CPU port) on all host
+    threads over the first reads of the workload, sized to ~target_s seconds.
+    Returns the baseline record, the oracle's batch for those reads (the
+    checker of the GPU result) and their count."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     pyoracle.build()
@@ -199,19 +203,33 @@ def cpu_baseline(prefix, seqs, offs, lens, k, smem, table, target_s=12.0, thread
 
     def run(n):
         t0 = time.perf_counter()
-        oidx.seed(seqs, offs[:n], lens[:n], k=k, smem=smem, pruned=True, threads=threads,
-                  table=table)
-        return time.perf_counter() - t0
+        b = oidx.seed(seqs, offs[:n], lens[:n], k=k, smem=smem, pruned=True, threads=threads,
+                      table=table)
+        return time.perf_counter() - t0, b
 
     n = min(20_000, n_total)
-    dt = run(n)
+    dt, batch = run(n)
     n2 = int(min(n_total, max(n, n / max(dt, 1e-3) * target_s)))
     if n2 > n:
-        dt = run(n2)
+        del batch
+        dt, batch = run(n2)
         n = n2
-    return {"value": n / dt, "unit": "reads/s", "cores": threads, "kind": "port",
-            "sample": f"first {n:,} reads of the workload, oracle containment-stopped walk, "
-                      f"{threads} threads, {dt:.1f}s"}
+    rec = {"value": n / dt, "unit": "reads/s", "cores": threads, "kind": "port",
+           "sample": f"first {n:,} reads of the workload, oracle containment-stopped walk, "
+                     f"{threads} threads, {dt:.1f}s"}
+    return rec, batch, n
+
+
+def parity_check(batch, res, n):
+    """reads among the first n whose GPU records (host result `res` of the
+    whole batch) differ from the oracle's"""
+    import pyoracle
+    t0 = time.perf_counter()
+    bad = pyoracle.mismatched_reads(batch, res.seeds, res.pos, res.read_seed_off,
+                                    res.read_pos_off, cols=(0, 1, 2, 3, 6))
+    log(f"[bench] parity: {n:,} reads checked against the oracle, {bad.size} differ "
+        f"({time.perf_counter() - t0:.1f}s)")
+    return int(bad.size)
 
 
 # --------------------------------------------------------------------------
@@ -374,6 +392,8 @@ def main():
     ap.add_argument("--no-text", action="store_true")
     ap.add_argument("--no-text-index", action="store_true",
                     help="seed without the full-SA / text structures")
+    ap.add_argument("--no-sampled-sa", action="store_true",
+                    help="skip the second timing without the text structures")
     ap.add_argument("--serve-slots", type=int, default=12)
     ap.add_argument("--serve-batch", type=int, default=1 << 18,
                     help="serving: most reads merged into one pass")
@@ -502,18 +522,17 @@ def main():
     log(f"[bench] plain: {pms / args.plain_steps:.1f} ms/step, {plain_value:,.0f} reads/s, "
         f"search {statistics.mean(psearch):.1f} ms")
 
-    # algorithmic work of the canonical walk, counted on the whole workload
+    # work the search executes with its own start table, counted on the whole
+    # workload: the plain kernel's walk is the canonical containment-stopped
+    # walk from that table; the batched search's own lookups beside it
     step(gs.KERNEL_PLAIN, count=True)
     torch.cuda.synchronize()
     work = ctx.last_work()
-    # lookups the batched search executes (helper lanes, steps before a kill
-    # is seen, walks in the tail pass), same knobs
     step(gs.KERNEL_BATCHED, count=True)
     torch.cuda.synchronize()
     executed = ctx.last_work()
-    search_bytes = 32 * (work["n_kmer"] + work["n_occ_blocks"])
+    own_bytes = 32 * (work["n_kmer"] + work["n_occ_blocks"])
     mean_search_s = statistics.mean(search_ms) / 1e3
-    achieved = search_bytes / mean_search_s / 1e9
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -535,15 +554,6 @@ def main():
                                          C.POINTER(C.c_double)]
     g32 = C.c_double()
     gs.check(L.gs_probe_random_gather(local, 16 << 30, 32, 1 << 30, C.byref(g32)))
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic,
-                "peak_source": f"{peak_src} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
-                "kernel": "gs_search_start + gs_search_walk + gs_search_text (one search pass)",
-                "algorithmic_bytes_per_launch": search_bytes,
-                "random_32B_gather_gbs": g32.value,
-                "frac_of_random_32B": achieved / g32.value if g32.value else None}
-    log(f"[bench] search {achieved:.0f} GB/s algorithmic = {achieved / peak:.3f} of {peak:.0f} GB/s; "
-        f"random 32B gather {g32.value:.0f} GB/s")
 
     # e2e through the C-ABI with pinned host buffers
     h_seqs = torch.from_numpy(seqs).pin_memory()
@@ -560,7 +570,7 @@ def main():
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = max(1, args.steps)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         gs.check(L.gs_seed(ctx.h, C2.c_void_p(hs.ctypes.data), C2.c_void_p(ho.ctypes.data),
@@ -605,18 +615,92 @@ def main():
         latency = serving_sweep(idx, w["codes"], w["nmask"], k, smem, value / ws,
                                 max_batch_reads=args.serve_batch, n_slots=args.serve_slots)
 
-    cpu = None
+    def device_pass_result():
+        """host copy of one batched pass over the whole workload"""
+        ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), n_reads,
+                        fetch=True, k=k, smem=smem, **knobs)
+        return ctx.result()
+
+    # CPU baseline: the oracle on the first reads of the workload; its output
+    # is also the checker of the GPU's records for those reads, and its work
+    # counters give the canonical walk's lookups from the 13-mer table
+    cpu, parity, canon = None, None, None
+    oracle_batch, n_checked = None, 0
     if rank == 0 and not args.no_cpu_baseline:
         table = idx.kmer_table()
-        cpu = cpu_baseline(w["prefix"], seqs, offs, lens, k, smem, table)
+        cpu, oracle_batch, n_checked = cpu_baseline(w["prefix"], seqs, offs, lens, k, smem, table)
+        del table
         log(f"[bench] cpu baseline: {cpu['value']:,.0f} reads/s on {cpu['cores']} threads")
+        parity = {"reads_checked": n_checked,
+                  "mismatches": parity_check(oracle_batch, device_pass_result(), n_checked),
+                  "checker": "oracle containment-stopped walk, exact seeds (x, y, l, u, count) "
+                             "and positions of the first reads of the workload"}
+        # candidates of the sample and of the whole workload scale the counts
+        cand = np.maximum(lens.astype(np.int64) - (k - 1), 0)
+        scale = float(cand.sum()) / max(1.0, float(cand[:n_checked].sum()))
+        ow = oracle_batch.work
+        canon = {"n_kmer": ow["n_kmer"] * scale, "n_occ_blocks": ow["n_occ_blocks"] * scale,
+                 "sample_reads": n_checked, "scale": scale}
+
+    # roofline of the search pass.  achieved = the canonical walk's bytes from
+    # the 13-mer table (32 B per table sector and per occurrence block, the
+    # implementation-independent count; from the oracle's sample, scaled by
+    # candidates) / the search kernels' CUDA-event time; the same from the
+    # start table this index uses (the plain kernel's count over the whole
+    # workload) beside it
+    canon_bytes = 32 * (canon["n_kmer"] + canon["n_occ_blocks"]) if canon else None
+    own_achieved = own_bytes / mean_search_s / 1e9
+    achieved = canon_bytes / mean_search_s / 1e9 if canon_bytes else own_achieved
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "peak_source": f"{peak_src} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
+                "kernel": "gs_search_start + gs_search_walk + gs_search_text (one search pass)",
+                "algorithmic_bytes_per_launch": canon_bytes if canon_bytes else own_bytes,
+                "algorithmic_count": ("canonical containment-stopped walk from the 13-mer table "
+                                      "(oracle sample, scaled by candidates)") if canon_bytes else
+                                     f"canonical walk from the {idx.info().kmer_len}-mer start table",
+                "own_start_table": {"kmer_len": idx.info().kmer_len, "bytes": own_bytes,
+                                    "achieved": own_achieved, "frac": own_achieved / peak},
+                "random_32B_gather_gbs": g32.value,
+                "frac_of_random_32B": achieved / g32.value if g32.value else None}
+    log(f"[bench] search {achieved:.0f} GB/s algorithmic = {achieved / peak:.3f} of {peak:.0f} GB/s "
+        f"({own_achieved:.0f} GB/s from the {idx.info().kmer_len}-mer start table); "
+        f"random 32B gather {g32.value:.0f} GB/s")
+
+    # the headline's index state, before the sampled-SA timing frees the
+    # text structures
+    cfg_d = config_dict(args, w)
+    text_on = idx.info().text_min > 0
+
+    # the sampled-SA walk (no text structures): locate by LF steps to a
+    # sampled row, no text mode; same graph-replayed pass, timed the same way
+    sampled = None
+    if not args.no_text_index and not args.no_sampled_sa:
+        idx.set_text(0)
+        sms, _ = timed(gs.KERNEL_BATCHED, args.steps, args.warmup, None, graph=True)
+        sms = max_over_ranks(dist, sms, dev)
+        ssearch = []
+        for _ in range(3):
+            step(gs.KERNEL_BATCHED)
+            ssearch.append(ctx.last_timing()[0])
+        sampled = {"value": sum_over_ranks(dist, n_reads * args.steps, dev) / (sms / 1e3),
+                   "unit": "reads/s",
+                   "ms_per_step": sms / args.steps, "search_ms": statistics.mean(ssearch[1:]),
+                   "index": "no text structures: locate walks LF steps to a sampled SA row"}
+        if oracle_batch is not None:
+            sampled["parity"] = {"reads_checked": n_checked,
+                                 "mismatches": parity_check(oracle_batch, device_pass_result(),
+                                                            n_checked)}
+        log(f"[bench] sampled-SA walk: {sms / args.steps:.1f} ms/step, "
+            f"{sampled['value']:,.0f} reads/s, search {sampled['search_ms']:.1f} ms")
+    del oracle_batch
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": config_dict(args, w),
+            "config": cfg_d,
             "plain": {"value": plain_value, "unit": "reads/s", "ms_per_step": pms / args.plain_steps,
                       "search_ms": statistics.mean(psearch)},
             "batched_over_plain": value / plain_value,
@@ -628,6 +712,7 @@ def main():
                         "handed_to_text_pass": text_jobs, "text_buffer": text_cap},
             "text": text,
             "work": work,
+            "work_canonical_13mer": canon,
             "work_executed_batched": {"n_kmer": executed["n_kmer"],
                                       "n_occ_blocks": executed["n_occ_blocks"],
                                       "over_canonical": (executed["n_kmer"] + executed["n_occ_blocks"]) /
@@ -635,11 +720,13 @@ def main():
             "e2e": {"value": e2e_value, "unit": "reads/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             # prepare, start, walk, (text), finalize count + emit, expand, locate
-            "gpu_launches": (8 if idx.info().text_min > 0 else 7) * args.steps,
+            "gpu_launches": (8 if text_on else 7) * args.steps,
             "graph": "each timed step replays one CUDA graph of the whole pass",
             "clocks": clocks.summary(),
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "parity": parity,
+            "sampled_sa": sampled,
             "latency": latency,
         }
         line["config"]["autotuned"] = knobs

@@ -213,3 +213,42 @@ class Batch:
             out.append((x, y, l, u, self.pos[p:p + n].tolist()))
             p += n
         return out
+
+
+def _ranges(starts, counts):
+    """concatenation of arange(starts[i], starts[i] + counts[i]) and the read
+    index of each element"""
+    counts = counts.astype(np.int64)
+    tot = int(counts.sum())
+    reads = np.repeat(np.arange(counts.size, dtype=np.int64), counts)
+    first = np.cumsum(counts) - counts
+    return starts.astype(np.int64)[reads] + (np.arange(tot, dtype=np.int64) - first[reads]), reads
+
+
+def mismatched_reads(ob: Batch, seeds, pos, read_seed_off, read_pos_off, r0=0,
+                     cols=(0, 1, 2, 3, 4)) -> np.ndarray:
+    """Reads of the oracle batch `ob` (its read i = read r0 + i of the other
+    result) whose seeds or positions differ from the other result's: seed
+    rows whose columns `cols` are [x, y, l, u, n_pos] (uint32; (0, 1, 2, 3, 6)
+    for the library's gs_seed_rec rows), positions, and per-read offsets
+    (n_reads + 1 entries).  Exact comparison, vectorised; returns the batch's
+    read indices that differ."""
+    n = ob.n_reads
+    gso = np.asarray(read_seed_off[r0:r0 + n + 1], dtype=np.int64)
+    gpo = np.asarray(read_pos_off[r0:r0 + n + 1], dtype=np.int64)
+    oso = ob.read_seed_off[:n + 1].astype(np.int64)
+    opo = ob.read_pos_off[:n + 1].astype(np.int64)
+    ons, onp = np.diff(oso), np.diff(opo)
+    bad = (np.diff(gso) != ons) | (np.diff(gpo) != onp)
+    ok = ~bad
+    oi, reads = _ranges(oso[:-1], np.where(ok, ons, 0))
+    gi, _ = _ranges(gso[:-1], np.where(ok, ons, 0))
+    if oi.size:
+        rowbad = np.any(np.asarray(seeds)[gi][:, list(cols)] != ob.seeds[oi], axis=1)
+        bad[np.unique(reads[rowbad])] = True
+    oi, reads = _ranges(opo[:-1], np.where(ok, onp, 0))
+    gi, _ = _ranges(gpo[:-1], np.where(ok, onp, 0))
+    if oi.size:
+        posbad = np.asarray(pos)[gi] != ob.pos[oi]
+        bad[np.unique(reads[posbad])] = True
+    return np.nonzero(bad)[0]
