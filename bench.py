@@ -398,6 +398,9 @@ def main():
     ap.add_argument("--serve-batch", type=int, default=1 << 18,
                     help="serving: most reads merged into one pass")
     ap.add_argument("--retune", action="store_true")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="profiling driver: default launch knobs, W + K uncaptured batched "
+                         "passes (the K inside the NVTX range timed_batched), nothing else")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -429,6 +432,38 @@ def main():
     d_offs = torch.from_numpy(offs.view(np.int64)).to(dev)
     d_lens = torch.from_numpy(lens.view(np.int32)).to(dev)
     torch.cuda.synchronize()
+
+    if args.kernels_only:
+        # one kernel launch per pass stage, visible to a profiler by name
+        for _ in range(args.warmup):
+            ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), n_reads,
+                            fetch=False, k=k, smem=smem)
+        torch.cuda.synchronize()
+        nvtx("timed_batched")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(args.steps):
+            ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), n_reads,
+                            fetch=False, k=k, smem=smem)
+        e1.record(st)
+        torch.cuda.synchronize()
+        nvtx(None)
+        walkers, text_jobs = ctx.last_walkers(), ctx.last_text_jobs()
+        ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), n_reads,
+                        fetch=False, k=k, smem=smem, count_work=True)
+        torch.cuda.synchronize()
+        executed = ctx.last_work()
+        ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), n_reads,
+                        fetch=False, k=k, smem=smem, count_work=True, kernel=gs.KERNEL_PLAIN)
+        torch.cuda.synchronize()
+        print(json.dumps({"kernels_only": True, "reads": n_reads, "ref_bp": int(w["spec"].length),
+                          "kmer_start_len": idx.info().kmer_len,
+                          "device_bytes_index": idx.info().device_bytes,
+                          "ms_per_step": e0.elapsed_time(e1) / args.steps,
+                          "work_executed_batched": executed, "work_canonical_own": ctx.last_work(),
+                          "walkers": walkers, "text_jobs": text_jobs}),
+              flush=True)
+        return
 
     # autotuned launch knobs of the batched search (cached per GPU and workload)
     tag = f"{torch.cuda.get_device_name(local)}|cfg{args.config}|{w['spec'].length}|{n_reads}|{k}|{smem}"

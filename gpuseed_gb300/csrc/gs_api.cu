@@ -217,7 +217,7 @@ extern "C" int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out)
 {
     if (!idx || !out) return GS_EINVAL;
     *out = NULL;
-    GS_CUDA(cudaSetDevice(gs_index_device(idx)));
+    GS_ON_DEVICE(gs_index_device(idx));
     gs_ctx *c = (gs_ctx *)calloc(1, sizeof(gs_ctx));
     if (!c) return GS_ENOMEM;
     c->idx = idx;
@@ -847,7 +847,7 @@ extern "C" int gs_seed_device(gs_ctx *c, const char *d_seqs, const uint64_t *d_o
         return GS_EINVAL;
     }
     RC(check_params(p));
-    GS_CUDA(cudaSetDevice(gs_index_device(c->idx)));
+    GS_ON_DEVICE(gs_index_device(c->idx));
     if (p->graph && p->kernel == GS_KERNEL_BATCHED && !p->count_work && n_reads)
         return run_graph(c, d_seqs, d_offsets, d_lengths, n_reads, p, fetch_to_host);
     return run_pipeline(c, d_seqs, d_offsets, d_lengths, n_reads, p, fetch_to_host);
@@ -949,7 +949,7 @@ extern "C" int gs_seed(gs_ctx *c, const char *seqs, const uint64_t *offsets,
         return GS_EINVAL;
     }
     RC(check_params(p));
-    GS_CUDA(cudaSetDevice(gs_index_device(c->idx)));
+    GS_ON_DEVICE(gs_index_device(c->idx));
     /* offsets and lengths first; the end of the last base comes from a
      * reduction on the device, then the bases themselves */
     RC(grow(c->d_offsets, c->cap_offsets, (size_t)n_reads + 1, c->st));
@@ -1226,7 +1226,7 @@ extern "C" int gs_autotune(gs_ctx *c, const char *d_seqs, const uint64_t *d_offs
         return GS_EINVAL;
     }
     RC(check_params(p));
-    GS_CUDA(cudaSetDevice(gs_index_device(c->idx)));
+    GS_ON_DEVICE(gs_index_device(c->idx));
     uint32_t n = sample && sample < n_reads ? sample : n_reads;
     auto eval = [&](const gs_params &q, float &ms) -> int {
         float best = 1e30f;

@@ -366,7 +366,7 @@ extern "C" int gs_index_build(const uint8_t *codes, uint64_t n, uint32_t sa_intv
             gs_set_error("gs_index_build: code %u at %llu is not 0..3", codes[i], (unsigned long long)i);
             return GS_EINVAL;
         }
-    GS_CUDA(cudaSetDevice(device));
+    GS_ON_DEVICE(device);
     uint32_t primary = 0, L2[4];
     uint32_t *bwt = NULL, *smp = NULL;
     uint64_t words = 0, n_samples = 0;

@@ -213,7 +213,7 @@ static int upload(uint32_t primary, const uint32_t L2_1to4[4], const uint32_t *b
                      (unsigned long long)(n_sa - 1));
         return GS_EFORMAT;
     }
-    GS_CUDA(cudaSetDevice(device));
+    GS_ON_DEVICE(device);
     gs_index *idx = (gs_index *)calloc(1, sizeof(gs_index));
     if (!idx) return GS_ENOMEM;
     idx->device = device;
@@ -402,7 +402,7 @@ extern "C" int gs_index_text_table(const gs_index *idx, int which, uint64_t firs
         return GS_EINVAL;
     }
     const uint32_t *src = which == 0 ? idx->d_saf : which == 1 ? idx->d_text : idx->d_isa;
-    GS_CUDA(cudaSetDevice(idx->device));
+    GS_ON_DEVICE(idx->device);
     GS_CUDA(cudaMemcpy(out, src + first, count * 4, cudaMemcpyDeviceToHost));
     return GS_OK;
 }
@@ -423,7 +423,7 @@ static void drop_text(gs_index *idx)
 extern "C" int gs_index_set_text(gs_index *idx, int min_steps)
 {
     if (!idx) return GS_EINVAL;
-    GS_CUDA(cudaSetDevice(idx->device));
+    GS_ON_DEVICE(idx->device);
     GS_CUDA(cudaDeviceSynchronize());
     idx->gen++;
     if (min_steps == 0) {
@@ -473,7 +473,7 @@ extern "C" int gs_index_kmer_table(const gs_index *idx, uint64_t first, uint64_t
                      (unsigned long long)count, (unsigned long long)n);
         return GS_EINVAL;
     }
-    GS_CUDA(cudaSetDevice(idx->device));
+    GS_ON_DEVICE(idx->device);
     GS_CUDA(cudaMemcpy(out, idx->d_kmer + first, count * 8, cudaMemcpyDeviceToHost));
     return GS_OK;
 }
@@ -491,7 +491,7 @@ extern "C" int gs_index_set_kmer_len(gs_index *idx, int kx)
         gs_set_error("k-mer start table length %d outside [13, 16]", kx);
         return GS_EINVAL;
     }
-    GS_CUDA(cudaSetDevice(idx->device));
+    GS_ON_DEVICE(idx->device);
     GS_CUDA(cudaDeviceSynchronize());
     idx->gen++;
     if (idx->d_kmerx) {

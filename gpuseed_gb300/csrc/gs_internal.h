@@ -163,6 +163,31 @@ int gs_cuda_fail(cudaError_t e, const char *what);
         if (_e != cudaSuccess) return gs_cuda_fail(_e, #call); \
     } while (0)
 
+/* Makes a device current for the rest of the scope and gives the calling
+ * thread its previous current device back on every return path, so that a
+ * library call does not leave a C caller that drives several GPUs from one
+ * thread on another device. */
+struct GsDeviceGuard {
+    int prev = -1;
+    bool changed = false;
+    cudaError_t enter(int dev)
+    {
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) return e;
+        if (prev == dev) return cudaSuccess;
+        e = cudaSetDevice(dev);
+        changed = e == cudaSuccess;
+        return e;
+    }
+    ~GsDeviceGuard()
+    {
+        if (changed) cudaSetDevice(prev);
+    }
+};
+#define GS_ON_DEVICE(dev)            \
+    GsDeviceGuard gs_device_guard_;  \
+    GS_CUDA(gs_device_guard_.enter(dev))
+
 /* kernel launchers (defined next to their kernels) */
 int gs_build_kmer_table(const GsDevIndex &idx, uint2 *table, cudaStream_t st);
 int gs_launch_text_lengths(const GsTextArgs &a, cudaStream_t st);

@@ -12,10 +12,18 @@
  * until the process exits.  The caller passes the reads and the output
  * buffers; results are written only there.
  *
+ * The search is the lockstep form without the tail-pass hand-over
+ * (GS_KERNEL_LOCKSTEP with handoff_lanes < 0): it needs neither the walker
+ * buffer of the batched form nor the hand-over records, whose sizes follow
+ * the batch.  Its seeds and positions are the same integers.
+ *
  * Host code must not use the array's name as a device address: on the host
  * it names a shadow object.  The device address is taken once per device
  * with cudaGetSymbolAddress, with that device current, on the first call
  * made on that device -- make that first call before any stream capture.
+ * The address is kept for the life of the process, so the device must not
+ * be reset (cudaDeviceReset) between calls.  Each call synchronises its
+ * stream three times, to size the pass from counts on the device.
  *
  * All calls share the one array and leave their data in it; each call
  * clears what has to start at zero.  Calls whose work overlaps on the GPU
@@ -88,8 +96,9 @@ extern "C" int gs_seed_noalloc(gs_index *idx, const char *d_seqs, const uint64_t
         gs_set_error("gs_seed_noalloc: null argument");
         return GS_EINVAL;
     }
-    if (p->kernel != GS_KERNEL_BATCHED) {
-        gs_set_error("gs_seed_noalloc runs the batched search only");
+    if (p->kernel != GS_KERNEL_BATCHED && p->kernel != GS_KERNEL_LOCKSTEP) {
+        gs_set_error("gs_seed_noalloc: kernel must be GS_KERNEL_BATCHED or GS_KERNEL_LOCKSTEP "
+                     "(both run the lockstep search here)");
         return GS_EINVAL;
     }
     if (p->k < GS_K0 || (p->n_mode != GS_N_WILDCARD && p->n_mode != GS_N_STOP) ||
@@ -103,7 +112,7 @@ extern "C" int gs_seed_noalloc(gs_index *idx, const char *d_seqs, const uint64_t
         return GS_EINVAL;
     }
     const int dev = gs_index_device(idx);
-    GS_CUDA(cudaSetDevice(dev));
+    GS_ON_DEVICE(dev);
     unsigned char *scratch = NULL;
     NA_RC(scratch_address(dev, &scratch));
     cudaStream_t st = (cudaStream_t)cuda_stream;
@@ -169,8 +178,10 @@ extern "C" int gs_seed_noalloc(gs_index *idx, const char *d_seqs, const uint64_t
     B.recmask = recmask;
     GS_CUDA(cudaMemsetAsync(recmask, 0, ((n_slots + 31) / 32 + 1) * sizeof(uint32_t), st));
     B.item_cap = n_items;
-    /* the lockstep form: it needs no walker buffer */
-    NA_RC(gs_launch_search(I, B, GS_KERNEL_LOCKSTEP, p->queue_chunk, p->ctas_per_sm, n_items, st));
+    /* the lockstep form without hand-over (B.cont stays NULL): it needs no
+     * walker buffer and no hand-over records; its launch knobs are its own
+     * defaults, not the caller's, which are tuned for the batched form */
+    NA_RC(gs_launch_search(I, B, GS_KERNEL_LOCKSTEP, 0, 0, n_items, st));
 
     /* filters and counts; offsets go straight to the caller's arrays */
     B.rd_nf = rd_nf;

@@ -253,7 +253,7 @@ extern "C" int gs_server_start(gs_index *idx, const gs_server_opts *opts, gs_ser
     s->reserved = 0;
     s->start_error = 0;
     memset(&s->stats, 0, sizeof(s->stats));
-    GS_CUDA(cudaSetDevice(gs_index_device(idx)));
+    GS_ON_DEVICE(gs_index_device(idx));
     size_t free_b = 0, total_b = 0;
     GS_CUDA(cudaMemGetInfo(&free_b, &total_b));
     s->budget = opts->hbm_budget ? opts->hbm_budget : (uint64_t)(free_b * 0.6);

@@ -95,7 +95,7 @@ extern "C" int gs_probe_random_gather_mode(int device, uint64_t bytes, uint32_t 
         gs_set_error("gs_probe_random_gather_mode: mode 0-9, bytes >= 1024, n_loads > 0");
         return GS_EINVAL;
     }
-    GS_CUDA(cudaSetDevice(device));
+    GS_ON_DEVICE(device);
     int sms = 0;
     GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     uint32_t *buf = NULL, *sink = NULL;
@@ -135,7 +135,7 @@ extern "C" int gs_probe_random_gather(int device, uint64_t bytes, uint32_t load_
         gs_set_error("gs_probe_random_gather: load_bytes 32|64, bytes >= 1024, n_loads > 0");
         return GS_EINVAL;
     }
-    GS_CUDA(cudaSetDevice(device));
+    GS_ON_DEVICE(device);
     int sms = 0;
     GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     uint32_t *buf = NULL, *sink = NULL;
@@ -175,7 +175,7 @@ extern "C" int gs_set_l2_fetch_granularity(int device, int bytes)
         gs_set_error("L2 fetch granularity must be 32, 64 or 128 bytes");
         return GS_EINVAL;
     }
-    GS_CUDA(cudaSetDevice(device));
+    GS_ON_DEVICE(device);
     if (bytes) GS_CUDA(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)bytes));
     size_t v = 0;
     GS_CUDA(cudaDeviceGetLimit(&v, cudaLimitMaxL2FetchGranularity));

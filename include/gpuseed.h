@@ -13,7 +13,9 @@
  * gs_index_set_kmer_len / _set_text / _set_l2_window, which must not overlap
  * a pass on any of its contexts (a context's captured pass is captured
  * again after such a change).  A gs_ctx (stream + workspace + last result)
- * belongs to one host thread at a time.
+ * belongs to one host thread at a time.  A call makes its index's device
+ * current while it runs and gives the calling thread its previous current
+ * device back before it returns.
  */
 #ifndef GPUSEED_H
 #define GPUSEED_H
@@ -286,18 +288,24 @@ int gs_server_replay(gs_server *srv, const char *pool_seqs, const uint64_t *pool
  * No counterpart in the reference.  For callers that may not allocate device
  * memory while they run (a process that fixed its HBM budget at start-up, or
  * one that cannot let cudaMalloc/cudaFree synchronise the device under other
- * streams' work): the same batched pass as gs_seed_device, with every scratch
- * buffer inside one static device array of GS_NOALLOC_SCRATCH_BYTES that the
- * library keeps on each GPU that loads it.  It allocates nothing; the caller
- * passes device reads and device output buffers (seeds, positions, per-read
- * offsets of n_reads + 1 entries) and gets the counts in *n_seeds_out and
- * *n_pos_out.  Limits per call: GS_NOALLOC_MAX_READS reads,
- * GS_NOALLOC_MAX_SLOTS candidate slots (2 per start position), seeds and
- * positions as below; larger inputs are rejected with GS_EINVAL, larger
- * results with GS_EOVERFLOW (counts still reported).  The first call on a
- * device looks up the array's device address; make it before any stream
- * capture.  Calls share the array: calls that overlap on the GPU race, so
- * serialise them. */
+ * streams' work): a seeding pass whose every scratch buffer lies inside one
+ * static device array of GS_NOALLOC_SCRATCH_BYTES that the library keeps on
+ * each GPU that loads it.  The search is the lockstep form without its
+ * tail-pass hand-over (it needs no walker or hand-over buffer); the seeds,
+ * positions and offsets are the same integers gs_seed_device gives.  Of
+ * gs_params it reads k, smem, n_mode, lf_mode and max_occ; kernel must be
+ * GS_KERNEL_BATCHED or GS_KERNEL_LOCKSTEP, and the launch knobs are the
+ * lockstep form's defaults.  It allocates nothing; the caller passes device
+ * reads and device output buffers (seeds, positions, per-read offsets of
+ * n_reads + 1 entries) and gets the counts in *n_seeds_out and *n_pos_out.
+ * Limits per call: GS_NOALLOC_MAX_READS reads, GS_NOALLOC_MAX_SLOTS candidate
+ * slots (2 per start position), seeds and positions as below; larger inputs
+ * are rejected with GS_EINVAL, larger results with GS_EOVERFLOW (counts still
+ * reported).  The call synchronises its stream three times to size the pass.
+ * The first call on a device looks up the array's device address and keeps
+ * it; make that call before any stream capture, and do not reset the device
+ * (cudaDeviceReset) while the library is loaded.  Calls share the array:
+ * calls that overlap on the GPU race, so serialise them. */
 #define GS_NOALLOC_SCRATCH_BYTES (64u << 20)
 #define GS_NOALLOC_MAX_READS 65536u
 #define GS_NOALLOC_MAX_SLOTS (1u << 21)
