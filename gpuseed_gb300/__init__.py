@@ -20,6 +20,7 @@ CLI_PATH = os.path.join(_PKG, "seed_gen")
 N_WILDCARD, N_STOP = 0, 1
 LF_GPUSEED, LF_BWA = 0, 1
 KERNEL_BATCHED, KERNEL_PLAIN, KERNEL_LOCKSTEP = 0, 1, 2
+MEM_NEXT_READ, MEM_NEXT_GPUSEED = 0, 1
 
 GS_ERRORS = {-1: "EINVAL", -2: "EIO", -3: "EFORMAT", -4: "ENOMEM", -5: "ECUDA", -6: "EWALK",
              -7: "EOVERFLOW", -8: "ETIMEOUT", -9: "ESTATE"}
@@ -48,7 +49,7 @@ class Params(C.Structure):
                 ("lf_mode", C.c_int32), ("kernel", C.c_int32), ("queue_chunk", C.c_int32),
                 ("ctas_per_sm", C.c_int32), ("count_work", C.c_int32),
                 ("handoff_lanes", C.c_int32), ("handoff_steps", C.c_int32), ("graph", C.c_int32),
-                ("walker_slots", C.c_int32), ("max_occ", C.c_int32)]
+                ("walker_slots", C.c_int32), ("max_occ", C.c_int32), ("mem_next", C.c_int32)]
 
 
 class SeedRec(C.Structure):
@@ -278,10 +279,11 @@ class Context:
     @staticmethod
     def params(k=20, smem=False, n_mode=N_WILDCARD, lf_mode=LF_GPUSEED, kernel=KERNEL_BATCHED,
                queue_chunk=0, ctas_per_sm=0, count_work=False, handoff_lanes=0,
-               handoff_steps=0, graph=False, walker_slots=0, max_occ=0) -> Params:
+               handoff_steps=0, graph=False, walker_slots=0, max_occ=0,
+               mem_next=0) -> Params:
         return Params(k, 1 if smem else 0, n_mode, lf_mode, kernel, queue_chunk, ctas_per_sm,
                       1 if count_work else 0, handoff_lanes, handoff_steps, 1 if graph else 0,
-                      walker_slots, max_occ)
+                      walker_slots, max_occ, mem_next)
 
     def seed(self, seqs, offsets, lengths, **kw) -> Result:
         """Reads in host memory; returns the host result."""

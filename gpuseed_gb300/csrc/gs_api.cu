@@ -436,7 +436,8 @@ static int check_params(const gs_params *p)
     if ((p->n_mode != GS_N_WILDCARD && p->n_mode != GS_N_STOP) ||
         (p->lf_mode != GS_LF_GPUSEED && p->lf_mode != GS_LF_BWA) ||
         (p->kernel != GS_KERNEL_BATCHED && p->kernel != GS_KERNEL_PLAIN &&
-         p->kernel != GS_KERNEL_LOCKSTEP)) {
+         p->kernel != GS_KERNEL_LOCKSTEP) ||
+        (p->mem_next != GS_MEM_NEXT_READ && p->mem_next != GS_MEM_NEXT_GPUSEED)) {
         gs_set_error("gs_params mode out of range");
         return GS_EINVAL;
     }
@@ -484,6 +485,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     B.n_mode = p->n_mode;
     B.lf_mode = p->lf_mode;
     B.max_occ = p->max_occ > 0 ? (uint32_t)p->max_occ : 0u;
+    B.mem_next = p->mem_next;
     B.queue = c->queue;
     B.work = p->count_work ? c->d_work : NULL;
     memset(c->work, 0, sizeof(c->work));
@@ -718,6 +720,7 @@ static int enqueue_pass(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     B.n_mode = p->n_mode;
     B.lf_mode = p->lf_mode;
     B.max_occ = p->max_occ > 0 ? (uint32_t)p->max_occ : 0u;
+    B.mem_next = p->mem_next;
     B.queue = c->queue;
     GS_CUDA(cudaMemsetAsync(c->queue, 0, 32, st));
     B.slot_off = c->slot_cnt;
@@ -967,7 +970,9 @@ extern "C" int gs_seed(gs_ctx *c, const char *seqs, const uint64_t *offsets,
         RC(fetch_small(&c->h_small[12], c->d_max, 16, c->st));
         GS_CUDA(cudaStreamSynchronize(c->st));
         bytes = c->h_small[12];
-        if (n_reads >= 2 * GS_SEED_CHUNK_READS && c->h_small[13] == 0)
+        /* chunks would cut the reference's cross-read neighbour scan */
+        const bool cross = !p->smem && p->mem_next == GS_MEM_NEXT_GPUSEED;
+        if (n_reads >= 2 * GS_SEED_CHUNK_READS && c->h_small[13] == 0 && !cross)
             return seed_chunked(c, seqs, offsets, n_reads, p, bytes);
     }
     RC(grow(c->d_seqs, c->cap_seqs, bytes + 1, c->st));

@@ -112,6 +112,7 @@ struct GsBatch {
     int32_t handoff_lanes;     /* hand over when at most this many owned lanes extend ... */
     int32_t handoff_steps;     /* ... after at least this many lockstep steps */
     uint32_t max_occ;          /* 0 or the largest interval an output seed may have */
+    int32_t mem_next;          /* GS_MEM_NEXT_READ | GS_MEM_NEXT_GPUSEED (MEM mode) */
     GsWalker *walkers;         /* batched search: survivors of the start pass */
     uint64_t walker_cap;       /* entries allocated (0: every walk stays in the start pass) */
     struct GsTextJob *text_jobs;   /* walkers handed to the text pass */

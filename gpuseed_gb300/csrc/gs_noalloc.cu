@@ -102,7 +102,8 @@ extern "C" int gs_seed_noalloc(gs_index *idx, const char *d_seqs, const uint64_t
         return GS_EINVAL;
     }
     if (p->k < GS_K0 || (p->n_mode != GS_N_WILDCARD && p->n_mode != GS_N_STOP) ||
-        (p->lf_mode != GS_LF_GPUSEED && p->lf_mode != GS_LF_BWA)) {
+        (p->lf_mode != GS_LF_GPUSEED && p->lf_mode != GS_LF_BWA) ||
+        (p->mem_next != GS_MEM_NEXT_READ && p->mem_next != GS_MEM_NEXT_GPUSEED)) {
         gs_set_error("gs_seed_noalloc: k must be >= 13 and modes in range");
         return GS_EINVAL;
     }
@@ -152,6 +153,7 @@ extern "C" int gs_seed_noalloc(gs_index *idx, const char *d_seqs, const uint64_t
     B.n_mode = p->n_mode;
     B.lf_mode = p->lf_mode;
     B.max_occ = p->max_occ > 0 ? (uint32_t)p->max_occ : 0u;
+    B.mem_next = p->mem_next;
     B.queue = queue;
     GS_CUDA(cudaMemsetAsync(queue, 0, 4 * sizeof(uint32_t), st));
 

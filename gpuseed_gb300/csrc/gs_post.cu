@@ -353,6 +353,69 @@ __global__ void __launch_bounds__(128) gs_finalize_emit(GsBatch B, uint64_t *see
     }
 }
 
+/* GS_MEM_NEXT_GPUSEED (MEM mode).  seeds_to_threads_mem (seed_gen.cu:635-650)
+ * looks for a kept record's exclusion interval among the compacted records
+ * that follow it (forward: same begin) or precede it (reverse: same end),
+ * and its scan does not stop at the read's end, while the count kernel's
+ * does (:927-989).  Inside the read the scan finds the filters' own
+ * neighbour.  It leaves the read only from the read's last forward record
+ * when the read has no reverse record -- into the next read that has
+ * records, whose first record is then forward -- and from the read's first
+ * reverse record when the read has no forward record, into the previous
+ * read's last record.  The record it meets heads (ends) a run whose last
+ * (first) record is kept, and a dropped record has the interval of the
+ * record it was dropped for, so the interval found is that of the other
+ * read's first forward (last reverse) output seed, when the begin (end)
+ * matches.  The seed keeps its count and its rows become the first n_pos
+ * rows from l outside that interval.  Thread per read, after the emit. */
+__global__ void __launch_bounds__(128) gs_mem_next_kernel(GsBatch B)
+{
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= B.n_reads) return;
+    const uint64_t s0 = B.seed_off[r], s1 = B.seed_off[r + 1];
+    if (s0 == s1 || s1 > B.seed_cap) return;
+    uint64_t last_f = s1, first_r = s1;
+    for (uint64_t s = s0; s < s1; s++) {
+        if ((uint32_t)B.seeds[s].y >> 31) {
+            if (first_r == s1) first_r = s;
+        } else {
+            last_f = s;
+        }
+    }
+    if (last_f < s1 && first_r == s1) {
+        /* the next read with seeds; its first seed in output order is
+         * forward exactly when it has forward records */
+        uint32_t q = r + 1;
+        while (q < B.n_reads && B.seed_off[q + 1] == B.seed_off[q]) q++;
+        if (q < B.n_reads && B.seed_off[q + 1] <= B.seed_cap) {
+            for (uint64_t s = B.seed_off[q]; s < B.seed_off[q + 1]; s++) {
+                const gs_seed_rec N = B.seeds[s];
+                if ((uint32_t)N.y >> 31) continue;
+                if (N.x == B.seeds[last_f].x) {
+                    B.seeds[last_f].xl = N.l;
+                    B.seeds[last_f].xu = N.u;
+                }
+                break;
+            }
+        }
+    }
+    if (first_r < s1 && last_f == s1 && r > 0) {
+        uint32_t q = r - 1;
+        while (q > 0 && B.seed_off[q + 1] == B.seed_off[q]) q--;
+        if (B.seed_off[q + 1] > B.seed_off[q] && B.seed_off[q + 1] <= B.seed_cap) {
+            for (uint64_t s = B.seed_off[q + 1]; s-- > B.seed_off[q];) {
+                const gs_seed_rec P = B.seeds[s];
+                if (!((uint32_t)P.y >> 31)) continue;
+                if (P.y == B.seeds[first_r].y) {
+                    B.seeds[first_r].xl = P.l;
+                    B.seeds[first_r].xu = P.u;
+                }
+                break;
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256) gs_expand(const uint64_t *seed_pos, const gs_seed_rec *seeds,
                                                  const uint64_t *n_seeds_dev, uint64_t seed_cap,
                                                  uint32_t *pmap, uint64_t pos_cap)
@@ -384,8 +447,10 @@ __global__ void __launch_bounds__(256) gs_locate(GsDevIndex I, const gs_seed_rec
         if (active) {
             uint32_t s = pmap[j];
             gs_seed_rec S = seeds[s];
+            /* the (j - first)-th row from l outside [xl, xu] */
             uint32_t row = S.l + (uint32_t)(j - seed_pos[s]);
-            if (S.xl <= S.xu && row >= S.xl) row += S.xu - S.xl + 1u;
+            const uint32_t x0 = S.xl > S.l ? S.xl : S.l;
+            if (S.xl <= S.xu && S.xu >= x0 && row >= x0) row += S.xu - x0 + 1u;
             /* locate_seeds_gpu (:668-684): LF until a sampled row; a
              * consistent index reaches one within seq_len+1 steps.  With
              * the full suffix array it is one read: the walk's result is
@@ -444,6 +509,10 @@ int gs_launch_finalize_emit(const GsDevIndex &I, GsBatch &B, cudaStream_t st)
     if (B.n_reads == 0) return GS_OK;
     gs_finalize_emit<<<(B.n_reads + 127) / 128, 128, 0, st>>>(B, B.seed_pos);
     GS_CUDA(cudaGetLastError());
+    if (!B.smem && B.mem_next == GS_MEM_NEXT_GPUSEED) {
+        gs_mem_next_kernel<<<(B.n_reads + 127) / 128, 128, 0, st>>>(B);
+        GS_CUDA(cudaGetLastError());
+    }
     return GS_OK;
 }
 

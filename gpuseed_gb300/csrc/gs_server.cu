@@ -242,6 +242,11 @@ extern "C" int gs_server_start(gs_index *idx, const gs_server_opts *opts, gs_ser
         return GS_EINVAL;
     }
     *out = NULL;
+    if (!opts->params.smem && opts->params.mem_next != GS_MEM_NEXT_READ) {
+        gs_set_error("gs_server_start: a request's seeds must not depend on the requests merged "
+                     "with it (mem_next must be GS_MEM_NEXT_READ)");
+        return GS_EINVAL;
+    }
     gs_server *s = new gs_server();
     s->idx = idx;
     s->opts = *opts;

@@ -19,7 +19,11 @@
  * line without a newline keeps its last base), -c INT (drop seeds that occur
  * more than INT times, as bwa's -c), -T (build the text structures:
  * full suffix array, packed text and inverse-SA samples; they cost ~0.5 s of
- * load on 3.1 Gbp and pay off above a few hundred million reads).  Errors
+ * load on 3.1 Gbp and pay off above a few hundred million reads), -Q (MEM
+ * mode: a read's exclusion interval may come from the neighbouring read of
+ * the batch, as seeds_to_threads_mem's scan finds it, seed_gen.cu:635-650;
+ * batches then default to the reference's 1,000,000 bases, :2955, so that
+ * the neighbours are the reference's).  Errors
  * print a message and exit with status 1, as the reference does for
  * unreadable index files.
  */
@@ -211,8 +215,8 @@ int main(int argc, char *argv[])
     memset(&p, 0, sizeof(p));
     p.k = 20;
     uint64_t batch_bases = 64u << 20;
-    int print_out = 0, records = 0, text = 0, c;
-    while ((c = getopt(argc, argv, "k:sonbPB:Fc:T")) >= 0) {
+    int print_out = 0, records = 0, text = 0, batch_set = 0, c;
+    while ((c = getopt(argc, argv, "k:sonbPB:Fc:TQ")) >= 0) {
         switch (c) {
         case 'k': p.k = atoi(optarg); break;
         case 's': p.smem = 1; break;
@@ -220,13 +224,15 @@ int main(int argc, char *argv[])
         case 'n': p.n_mode = GS_N_STOP; break;
         case 'b': p.lf_mode = GS_LF_BWA; break;
         case 'P': p.kernel = GS_KERNEL_PLAIN; break;
-        case 'B': batch_bases = strtoull(optarg, NULL, 10); break;
+        case 'B': batch_bases = strtoull(optarg, NULL, 10); batch_set = 1; break;
         case 'F': records = 1; break;
         case 'c': p.max_occ = atoi(optarg); break;
         case 'T': text = 1; break;
+        case 'Q': p.mem_next = GS_MEM_NEXT_GPUSEED; break;
         default: break;
         }
     }
+    if (p.mem_next && !batch_set) batch_bases = 1000000;
     if (optind + 2 > argc) {
         fprintf(stderr, "Usage: seed_gen [-k <minimum seed length>] [-s] [-o] <index prefix> "
                         "<reads fasta file>\n");

@@ -46,6 +46,20 @@ extern "C" {
 #define GS_LF_GPUSEED 0  /* LF(primary+1) = 0 as seed_gen.cu:455-458 */
 #define GS_LF_BWA 1      /* LF as bwa */
 
+/* MEM mode: where a kept record's exclusion interval (the nested interval of
+ * its neighbour toward the longer match) may come from. */
+#define GS_MEM_NEXT_READ 0     /* the same read only: a read's seeds do not depend on the
+                                  other reads of the batch (default; serving needs it) */
+#define GS_MEM_NEXT_GPUSEED 1  /* as seeds_to_threads_mem (seed_gen.cu:635-650), whose scan
+                                  for the neighbour does not stop at the read's end: a
+                                  read's last forward seed, when the read has no reverse
+                                  seed, takes the first forward seed of the next read with
+                                  seeds if it has the same begin (and a read's first
+                                  reverse seed, when the read has no forward seed, the
+                                  last reverse seed of the previous one if it has the
+                                  same end); it keeps its count and emits the first
+                                  n_pos rows from l outside that interval */
+
 #define GS_KERNEL_BATCHED 0  /* candidates started a warp per work item, then walked one per
                                 lane, each with its neighbour's interval (default) */
 #define GS_KERNEL_PLAIN 1    /* one read per thread */
@@ -77,12 +91,17 @@ typedef struct {
     int32_t max_occ;        /* > 0: drop output seeds whose interval has more rows than this
                                (bwa's -c; applied after the filters, the other seeds are
                                unchanged); 0 = off, the reference's output */
+    int32_t mem_next;       /* GS_MEM_NEXT_READ | GS_MEM_NEXT_GPUSEED (MEM mode only; a
+                               batch then runs as one pass, and servers refuse it) */
 } gs_params;
 
 /* One output seed, in output order.  x/y are the reference's int2 read
  * position (begin, exclusive end; bit 31 of both set on the '-' strand,
- * seed_gen.cu:2262, :2402).  Its positions are rows [l,u] minus the nested
- * interval [xl,xu] (empty when xl > xu; MEM mode), n_pos of them. */
+ * seed_gen.cu:2262, :2402).  Its positions are the first n_pos rows from l
+ * that lie outside [xl,xu] (empty when xl > xu): rows [l,u] minus the nested
+ * interval [xl,xu] in MEM mode; with GS_MEM_NEXT_GPUSEED, [xl,xu] may be
+ * another read's interval that overlaps [l,u] without being nested, and the
+ * rows then run past u. */
 typedef struct {
     int32_t x, y;
     uint32_t l, u;
@@ -293,7 +312,7 @@ int gs_server_replay(gs_server *srv, const char *pool_seqs, const uint64_t *pool
  * each GPU that loads it.  The search is the lockstep form without its
  * tail-pass hand-over (it needs no walker or hand-over buffer); the seeds,
  * positions and offsets are the same integers gs_seed_device gives.  Of
- * gs_params it reads k, smem, n_mode, lf_mode and max_occ; kernel must be
+ * gs_params it reads k, smem, n_mode, lf_mode, max_occ and mem_next; kernel must be
  * GS_KERNEL_BATCHED or GS_KERNEL_LOCKSTEP, and the launch knobs are the
  * lockstep form's defaults.  It allocates nothing; the caller passes device
  * reads and device output buffers (seeds, positions, per-read offsets of

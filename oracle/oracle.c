@@ -592,6 +592,66 @@ static int finish_read(const or_index *idx, const or_params *p, cand_rec *fw, in
     return OR_OK;
 }
 
+/* MEM mode, mem_next = 1: seeds_to_threads_mem (:635-650) scans for a
+ * record's exclusion interval through the batch's compacted records, past
+ * the read's end, while count_seed_intervals_gpu_mem (:927-989) counts
+ * within the read.  The scan leaves the read only from its last forward
+ * record when the read has no reverse record (the next array record is the
+ * next read's first; it matters when it is forward with the same begin) and
+ * from its first reverse record when the read has no forward record (the
+ * previous read's last record, reverse with the same end).  That record
+ * starts (ends) a run whose last (first) record is kept, and a dropped
+ * record has the interval of the one it was dropped for, so the first
+ * non-empty interval the scan meets is that of the other read's first
+ * forward (last reverse) output seed.  The seed keeps its count and its
+ * rows become the first n_pos rows from l outside that interval (the
+ * reference's emission loop, :655-662).  Runs after every read is done. */
+static int mem_next_pass(const or_index *idx, const or_params *p, or_batch *bt)
+{
+    for (uint32_t r = 0; r < bt->n_reads; r++) {
+        uint64_t s0 = bt->read_seed_off[r], s1 = bt->read_seed_off[r + 1];
+        if (s0 == s1) continue;
+        uint64_t last_f = s1, first_r = s1;
+        for (uint64_t s = s0; s < s1; s++) {
+            if ((uint32_t)bt->seeds[s].y >> 31) { if (first_r == s1) first_r = s; }
+            else last_f = s;
+        }
+        uint64_t target = s1;
+        const or_seed *J = NULL;
+        if (last_f < s1 && first_r == s1) {
+            uint32_t q = r + 1;
+            while (q < bt->n_reads && bt->read_seed_off[q + 1] == bt->read_seed_off[q]) q++;
+            if (q < bt->n_reads)
+                for (uint64_t s = bt->read_seed_off[q]; s < bt->read_seed_off[q + 1]; s++) {
+                    if ((uint32_t)bt->seeds[s].y >> 31) continue;
+                    if (bt->seeds[s].x == bt->seeds[last_f].x) { J = &bt->seeds[s]; target = last_f; }
+                    break;
+                }
+        } else if (first_r < s1 && last_f == s1 && r > 0) {
+            uint32_t q = r - 1;
+            while (q > 0 && bt->read_seed_off[q + 1] == bt->read_seed_off[q]) q--;
+            for (uint64_t s = bt->read_seed_off[q + 1]; s-- > bt->read_seed_off[q];) {
+                if (!((uint32_t)bt->seeds[s].y >> 31)) continue;
+                if (bt->seeds[s].y == bt->seeds[first_r].y) { J = &bt->seeds[s]; target = first_r; }
+                break;
+            }
+        }
+        if (!J) continue;
+        uint64_t pos = bt->read_pos_off[r];
+        for (uint64_t s = s0; s < target; s++) pos += bt->seeds[s].n_pos;
+        const or_seed *S = &bt->seeds[target];
+        uint32_t done = 0;
+        for (uint32_t row = S->l; done < S->n_pos; row++) {
+            if (row >= J->l && row <= J->u) continue;
+            uint32_t steps;
+            uint32_t v = or_locate(idx, row, p->lf_mode, &steps);
+            if (steps == (uint32_t)-1) return OR_EWALK;
+            bt->pos[pos + done++] = v;
+        }
+    }
+    return OR_OK;
+}
+
 /* ------------------------------------------------------------------ */
 /* batch driver */
 
@@ -739,6 +799,10 @@ int or_seed_batch(const or_index *idx, const uint32_t *table13,
                sizeof(or_seed) * bt->read_n_seeds[r]);
         memcpy(bt->pos + bt->read_pos_off[r], t->pos + c.read_pos_start[r],
                4 * c.read_n_pos[r]);
+    }
+    if (!p->smem && p->mem_next) {
+        rc = mem_next_pass(idx, p, bt);
+        if (rc) goto done;
     }
     for (int t = 0; t < n_threads; t++) {
         bt->n_kmer += wa[t].tb.w.n_kmer;

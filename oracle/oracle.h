@@ -57,6 +57,9 @@ typedef struct {
     int32_t smem;     /* -s: SMEM mode; 0 = MEM mode (seed_gen.cu:2831) */
     int32_t n_mode;   /* OR_N_WILDCARD / OR_N_STOP */
     int32_t lf_mode;  /* OR_LF_GPUSEED / OR_LF_BWA */
+    int32_t mem_next; /* 0: a MEM record's exclusion interval from its own read;
+                         1: also across reads, as seeds_to_threads_mem's scan
+                         (seed_gen.cu:635-650) finds it */
 } or_params;
 
 /* One output seed: the reference's int2 read position (x = begin, y = end

@@ -21,7 +21,8 @@ LF_GPUSEED, LF_BWA = 0, 1
 
 
 class _Params(C.Structure):
-    _fields_ = [("k", C.c_int32), ("smem", C.c_int32), ("n_mode", C.c_int32), ("lf_mode", C.c_int32)]
+    _fields_ = [("k", C.c_int32), ("smem", C.c_int32), ("n_mode", C.c_int32), ("lf_mode", C.c_int32),
+                ("mem_next", C.c_int32)]
 
 
 class _Seed(C.Structure):
@@ -153,12 +154,13 @@ class Index:
         return self._table
 
     def seed(self, seqs: bytes, offsets, lengths, k=20, smem=False, n_mode=N_WILDCARD,
-             lf_mode=LF_GPUSEED, pruned=False, threads=0, use_table=False, table=None) -> "Batch":
+             lf_mode=LF_GPUSEED, pruned=False, threads=0, use_table=False, table=None,
+             mem_next=0) -> "Batch":
         offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
         lengths = np.ascontiguousarray(lengths, dtype=np.uint32)
         buf = np.frombuffer(seqs, dtype=np.uint8) if isinstance(seqs, (bytes, bytearray)) else seqs
         buf = np.ascontiguousarray(buf, dtype=np.uint8)
-        p = _Params(k, 1 if smem else 0, n_mode, lf_mode)
+        p = _Params(k, 1 if smem else 0, n_mode, lf_mode, mem_next)
         out = C.POINTER(_Batch)()
         if table is None and use_table:
             table = self.table13(threads)

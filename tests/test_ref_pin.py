@@ -123,3 +123,46 @@ def test_random_sets_match_reference(built, tmp_path, case, init):
             print(f"case {case} init={init} k={k} smem={smem}: {excluded} of {lens.size} reads "
                   f"excluded (Q9)")
             assert not diff, (k, smem, diff[:5], ora[diff[0]] if diff else "", ref[diff[0]] if diff else "")
+
+
+def duplicate_pairs(codes, n_pairs, seed, L=80):
+    """reads in adjacent identical pairs, from both strands: the reference's
+    cross-read neighbour scan (seed_gen.cu:635-650) then meets the twin's
+    records"""
+    reads = sample_reads(codes, n_pairs, seed=seed, lengths=(L,), err=0.0)
+    out = []
+    for r in reads:
+        out += [r, r]
+    return out
+
+
+@pytest.mark.parametrize("init", INITS)
+def test_cross_read_mem_scan_matches_reference(built, tmp_path, init):
+    """MEM mode with mem_next = 1 reproduces the reference's cross-read
+    exclusion interval (quirk Q10); the default per-read mode differs from it
+    on these reads.  Reads whose neighbour lost its interval to Q9 are left
+    out with the Q9 reads themselves."""
+    pr = _need_ref()
+    codes = random_reference(40_000, 310, dups=10)
+    prefix = build_index(tmp_path, codes, sa_intv=7)
+    reads = duplicate_pairs(codes, 40, seed=9)
+    reads += sample_reads(codes, 40, seed=10, lengths=(60, 100, 150), err=0.02)
+    seqs, offs, lens = pack(reads)
+    ref_txt, nfwd = pr.run(prefix, seqs, offs, lens, 19, False, init, counts=True)
+    ref = per_read(ref_txt)
+    oidx = pyoracle.Index(prefix)
+    texts = {}
+    for mode in (0, 1):
+        b = oidx.seed(seqs, offs, lens, k=19, smem=False, mem_next=mode)
+        tmp = f"{prefix}.q10_{mode}.txt"
+        b.write_text(tmp, 1, False)
+        texts[mode] = per_read(open(tmp).read())
+    skip = {r for r in range(lens.size) if nfwd[r] == 1}
+    skip |= {r - 1 for r in skip if r > 0}
+    checked = [r for r in range(lens.size) if r not in skip]
+    diff = [r for r in checked if texts[1][r] != ref[r]]
+    assert not diff, (diff[:5], texts[1][diff[0]] if diff else "", ref[diff[0]] if diff else "")
+    per_read_mode = [r for r in checked if texts[0][r] != ref[r]]
+    print(f"init={init}: {len(checked)} reads compared, {len(skip)} left out (Q9); the per-read "
+          f"mode differs from the reference on {len(per_read_mode)}")
+    assert len(per_read_mode) >= 10
