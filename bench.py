@@ -453,6 +453,7 @@ def main():
                         fetch=False, k=k, smem=smem, count_work=True)
         torch.cuda.synchronize()
         executed = ctx.last_work()
+        walk_counts = ctx.last_walk_counts()
         ctx.seed_device(d_seqs.data_ptr(), d_offs.data_ptr(), d_lens.data_ptr(), n_reads,
                         fetch=False, k=k, smem=smem, count_work=True, kernel=gs.KERNEL_PLAIN)
         torch.cuda.synchronize()
@@ -461,7 +462,8 @@ def main():
                           "device_bytes_index": idx.info().device_bytes,
                           "ms_per_step": e0.elapsed_time(e1) / args.steps,
                           "work_executed_batched": executed, "work_canonical_own": ctx.last_work(),
-                          "walkers": walkers, "text_jobs": text_jobs}),
+                          "walkers": walkers, "text_jobs": text_jobs,
+                          "walk_counts": walk_counts}),
               flush=True)
         return
 
@@ -566,6 +568,7 @@ def main():
     step(gs.KERNEL_BATCHED, count=True)
     torch.cuda.synchronize()
     executed = ctx.last_work()
+    walk_counts = ctx.last_walk_counts()
     own_bytes = 32 * (work["n_kmer"] + work["n_occ_blocks"])
     mean_search_s = statistics.mean(search_ms) / 1e3
     peaks = {}
@@ -748,6 +751,7 @@ def main():
             "text": text,
             "work": work,
             "work_canonical_13mer": canon,
+            "walk_counts": walk_counts,
             "work_executed_batched": {"n_kmer": executed["n_kmer"],
                                       "n_occ_blocks": executed["n_occ_blocks"],
                                       "over_canonical": (executed["n_kmer"] + executed["n_occ_blocks"]) /

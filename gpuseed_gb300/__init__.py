@@ -117,6 +117,7 @@ def lib():
         L.gs_ctx_stream.restype = vp
         L.gs_ctx_last_timing.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         L.gs_ctx_last_work.argtypes = [vp, vp]
+        L.gs_ctx_last_walk_counts.argtypes = [vp, vp]
         L.gs_ctx_last_walkers.argtypes = [vp, C.POINTER(u64), C.POINTER(u64)]
         L.gs_ctx_last_text_jobs.argtypes = [vp, C.POINTER(u64), C.POINTER(u64)]
         L.gs_autotune.argtypes = [vp, vp, vp, vp, u32, C.POINTER(Params), u32, C.POINTER(C.c_float)]
@@ -345,6 +346,14 @@ class Context:
         a = np.zeros(4, dtype=np.uint64)
         check(lib().gs_ctx_last_work(self.h, _ptr(a)))
         return dict(n_kmer=int(a[0]), n_occ_blocks=int(a[1]), n_lf=int(a[2]), n_sa=int(a[3]))
+
+    def last_walk_counts(self):
+        """walk-pass counters of the last count_work batched pass"""
+        a = np.zeros(7, dtype=np.uint64)
+        check(lib().gs_ctx_last_walk_counts(self.h, _ptr(a)))
+        return dict(zip(("steps", "steps_with_j", "j_only_blocks", "j_steps_i_shrank",
+                         "walkers_with_j", "lines_256_rows", "lines_384_rows"),
+                        (int(v) for v in a)))
 
     def last_walkers(self):
         """(walkers handed to the walk pass, buffer capacity) of the last batched pass."""

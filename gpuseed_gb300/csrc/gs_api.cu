@@ -191,6 +191,7 @@ struct gs_ctx {
     uint64_t *d_max;
     unsigned long long *d_work;
     uint64_t work[4];
+    uint64_t walk_counts[7];   /* count_work pass: gs_ctx_last_walk_counts */
     void *cub_tmp; size_t cap_cub;
     uint64_t *h_small;          /* pinned scalars */
     /* host result */
@@ -241,7 +242,7 @@ extern "C" int gs_ctx_create(gs_index *idx, void *cuda_stream, gs_ctx **out)
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_d2h, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&c->queue, 32);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_max, 16);
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_work, 32);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_work, 128);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_small, 256);
     if (e != cudaSuccess) {
         int rc = gs_cuda_fail(e, "gs_ctx_create");
@@ -334,6 +335,13 @@ extern "C" int gs_ctx_last_work(gs_ctx *c, uint64_t out[4])
 {
     if (!c || !out) return GS_EINVAL;
     memcpy(out, c->work, sizeof(c->work));
+    return GS_OK;
+}
+
+extern "C" int gs_ctx_last_walk_counts(gs_ctx *c, uint64_t out[7])
+{
+    if (!c || !out) return GS_EINVAL;
+    memcpy(out, c->walk_counts, sizeof(c->walk_counts));
     return GS_OK;
 }
 
@@ -489,9 +497,10 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     B.queue = c->queue;
     B.work = p->count_work ? c->d_work : NULL;
     memset(c->work, 0, sizeof(c->work));
+    memset(c->walk_counts, 0, sizeof(c->walk_counts));
 
     GS_CUDA(cudaEventRecord(c->ev0, st));
-    if (B.work) GS_CUDA(cudaMemsetAsync(c->d_work, 0, 32, st));
+    if (B.work) GS_CUDA(cudaMemsetAsync(c->d_work, 0, 128, st));
     GS_CUDA(cudaMemsetAsync(c->queue, 0, 32, st));
     B.slot_off = c->slot_cnt;
     B.item_off = c->item_cnt;
@@ -633,6 +642,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     RC(fetch_small(&c->h_small[10], c->queue + 2, 4, st));
     RC(fetch_small(&c->h_small[11], c->queue + 4, 4, st));
     if (B.work) RC(fetch_small(&c->h_small[6], c->d_work, 32, st));
+    if (B.work) RC(fetch_small(&c->h_small[16], c->d_work + 4, 56, st));
     if (co) {
         /* after the small reads above: one copy engine serves both streams,
          * and this chunk's end should not wait for its own copy-out */
@@ -668,6 +678,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
         if (c->walker_per16 > 512u) c->walker_per16 = 512u;
     }
     if (B.work) memcpy(c->work, &c->h_small[6], sizeof(c->work));
+    if (B.work) memcpy(c->walk_counts, &c->h_small[16], sizeof(c->walk_counts));
     cudaEventElapsedTime(&c->t_search, c->ev_s0, c->ev_s1);
     cudaEventElapsedTime(&c->t_total, c->ev0, c->ev1);
     if (flags & GS_FLAG_WALK) {

@@ -1,13 +1,17 @@
 /*
  * gs_fm.cuh -- FM-index primitives on the device.
  *
- * One occurrence lookup = one 32-byte block = one 256-bit vector load
- * (ld.global.nc.v8.u32) of {4 checkpoint counts, 4 words of 2-bit BWT}.
- * The arithmetic is the reference's (seed_gen.cu:142-158 popcounts, :195-216
- * occ, :329-368 occ pair, :455-484 LF); the bit tricks are our own: a base
- * matches when its two bits XOR the replicated code are both zero, and the
- * bases after the queried row are removed with a mask instead of being
- * cleared and subtracted.
+ * The occurrence table in HBM: one 32-byte block per 64 rows of the
+ * $-removed BWT string, {count of A, C, G, T before the block, H0, H1, L0,
+ * L1}.  The counts are the reference's checkpoints (seed_gen.cu:52-58); the
+ * block's 64 bases are stored bit-sliced instead of as 2-bit fields: H0/H1
+ * hold their high bits and L0/L1 their low bits, base i of the block at bit
+ * 31 - (i & 31) of word i >> 5 of each.  The loader converts the file's
+ * packed words (16 bases per word, first base in the top bits) once
+ * (gs_index.cu).  The arithmetic is the reference's (seed_gen.cu:195-216
+ * occ, :329-368 occ pair, :455-484 LF); the counting is our own: the bases
+ * equal to c among the first n of a block are the set bits of
+ * (H ^ ~c1) & (L ^ ~c0) in the top n bits, two popcounts per query.
  */
 #ifndef GS_FM_CUH
 #define GS_FM_CUH
@@ -40,28 +44,50 @@ __device__ __forceinline__ uint32_t gs_L2(const GsDevIndex &I, uint32_t c)
     return gs_sel4(c, I.L2[0], I.L2[1], I.L2[2], I.L2[3]);
 }
 
-/* lanes of w (2-bit bases) equal to c, as the even bit of each pair */
-__device__ __forceinline__ uint32_t gs_match(uint32_t w, uint32_t c)
+/* bit-sliced match words of a block for base c: bit 31 - (i & 31) of word
+ * i >> 5 is set when base i of the block is c */
+struct GsMatch {
+    uint32_t cnt, m0, m1;
+};
+
+__device__ __forceinline__ GsMatch gs_match(uint32_t cnt, uint32_t h0, uint32_t h1, uint32_t l0,
+                                            uint32_t l1, uint32_t c)
 {
-    uint32_t x = w ^ (c * 0x55555555u);
-    return ~(x | (x >> 1)) & 0x55555555u;
+    const uint32_t hx = ((c >> 1) & 1u) - 1u;   /* ~0 when c's high bit is 0 */
+    const uint32_t lx = (c & 1u) - 1u;
+    GsMatch m;
+    m.cnt = cnt;
+    m.m0 = (h0 ^ hx) & (l0 ^ lx);
+    m.m1 = (h1 ^ hx) & (l1 ^ lx);
+    return m;
+}
+
+/* count of c in string positions [0, k] given k's block matched for c: the
+ * set bits among the top (k & 63) + 1 bits of m0:m1 */
+__device__ __forceinline__ uint32_t gs_occ_in_match(const GsMatch &m, uint32_t k)
+{
+    const uint32_t j = k & 63u;
+    const uint32_t c0 = __popc(m.m0 >> (31u - ((j & 31u) | ((j >> 5) * 31u))));
+    const uint32_t c1 = j >= 32u ? __popc(m.m1 >> (63u - j)) : 0u;
+    return m.cnt + c0 + c1;
 }
 
 /* count of c in string positions [0, k] given k's block */
 __device__ __forceinline__ uint32_t gs_occ_in_block(const GsBlk &b, uint32_t k, uint32_t c)
 {
-    uint32_t kw = (k >> 4) & 3u;
-    uint32_t tail = 0xffffffffu << ((15u - (k & 15u)) << 1);
-    uint32_t m0 = kw > 0 ? 0xffffffffu : tail;
-    uint32_t m1 = kw > 1 ? 0xffffffffu : (kw == 1 ? tail : 0u);
-    uint32_t m2 = kw > 2 ? 0xffffffffu : (kw == 2 ? tail : 0u);
-    uint32_t m3 = kw == 3 ? tail : 0u;
-    uint32_t n = gs_sel4(c, b.w[0], b.w[1], b.w[2], b.w[3]);
-    n += __popc(gs_match(b.w[4], c) & m0);
-    n += __popc(gs_match(b.w[5], c) & m1);
-    n += __popc(gs_match(b.w[6], c) & m2);
-    n += __popc(gs_match(b.w[7], c) & m3);
-    return n;
+    return gs_occ_in_match(gs_match(gs_sel4(c, b.w[0], b.w[1], b.w[2], b.w[3]), b.w[4], b.w[5],
+                                    b.w[6], b.w[7], c),
+                           k);
+}
+
+/* base at string position k given k's block */
+__device__ __forceinline__ uint32_t gs_block_base(const GsBlk &b, uint32_t k)
+{
+    const uint32_t sh = 31u - (k & 31u);
+    const bool hi = (k & 32u) != 0;
+    const uint32_t h = ((hi ? b.w[5] : b.w[4]) >> sh) & 1u;
+    const uint32_t l = ((hi ? b.w[7] : b.w[6]) >> sh) & 1u;
+    return (h << 1) | l;
 }
 
 /* One backward-search step with base c in [0,3]: [l,u] -> [l',u'].
@@ -98,10 +124,10 @@ __device__ __forceinline__ int gs_step(const GsDevIndex &I, uint32_t &l, uint32_
 }
 
 /* The part of a block one occurrence query with base c reads: the count
- * of c before the block and the four BWT words (a 4-byte and a 16-byte
- * load of the same 32-byte sector). */
+ * of c before the block and the four bit-slice words (a 4-byte and a
+ * 16-byte load of the same 32-byte sector). */
 struct GsHalf {
-    uint32_t cnt, w4, w5, w6, w7;
+    uint32_t cnt, h0, h1, l0, l1;
 };
 
 __device__ __forceinline__ GsHalf gs_load_half(const uint32_t *occ, uint32_t blk, uint32_t c)
@@ -110,7 +136,7 @@ __device__ __forceinline__ GsHalf gs_load_half(const uint32_t *occ, uint32_t blk
     const uint32_t *p = occ + (size_t)blk * GS_BLOCK_WORDS;
     asm("ld.global.nc.u32 %0, [%1];" : "=r"(h.cnt) : "l"(p + c));
     asm("ld.global.nc.v4.u32 {%0,%1,%2,%3}, [%4];"
-        : "=r"(h.w4), "=r"(h.w5), "=r"(h.w6), "=r"(h.w7)
+        : "=r"(h.h0), "=r"(h.h1), "=r"(h.l0), "=r"(h.l1)
         : "l"(p + 4));
     return h;
 }
@@ -119,36 +145,43 @@ __device__ __forceinline__ GsHalf gs_load_half(const uint32_t *occ, uint32_t blk
 __device__ __forceinline__ void gs_half_take(GsHalf &h, bool s, const GsHalf &a)
 {
     h.cnt = s ? a.cnt : h.cnt;
-    h.w4 = s ? a.w4 : h.w4;
-    h.w5 = s ? a.w5 : h.w5;
-    h.w6 = s ? a.w6 : h.w6;
-    h.w7 = s ? a.w7 : h.w7;
+    h.h0 = s ? a.h0 : h.h0;
+    h.h1 = s ? a.h1 : h.h1;
+    h.l0 = s ? a.l0 : h.l0;
+    h.l1 = s ? a.l1 : h.l1;
 }
 
 /* count of c in string positions [0, k] given k's block */
 __device__ __forceinline__ uint32_t gs_occ_in_half(const GsHalf &b, uint32_t k, uint32_t c)
 {
-    uint32_t kw = (k >> 4) & 3u;
-    uint32_t tail = 0xffffffffu << ((15u - (k & 15u)) << 1);
-    uint32_t m0 = kw > 0 ? 0xffffffffu : tail;
-    uint32_t m1 = kw > 1 ? 0xffffffffu : (kw == 1 ? tail : 0u);
-    uint32_t m2 = kw > 2 ? 0xffffffffu : (kw == 2 ? tail : 0u);
-    uint32_t m3 = kw == 3 ? tail : 0u;
-    uint32_t n = b.cnt;
-    n += __popc(gs_match(b.w4, c) & m0);
-    n += __popc(gs_match(b.w5, c) & m1);
-    n += __popc(gs_match(b.w6, c) & m2);
-    n += __popc(gs_match(b.w7, c) & m3);
-    return n;
+    return gs_occ_in_match(gs_match(b.cnt, b.h0, b.h1, b.l0, b.l1, c), k);
 }
+
+/* how many distinct values among those of a..d that are valid */
+__device__ __forceinline__ int gs_distinct4(uint32_t a, bool va, uint32_t b, bool vb, uint32_t c,
+                                            bool vc, uint32_t d, bool vd)
+{
+    return (int)va + (int)(vb && !(va && b == a)) + (int)(vc && !(va && c == a) && !(vb && c == b)) +
+           (int)(vd && !(va && d == a) && !(vb && d == b) && !(vc && d == c));
+}
+
+/* What one step of gs_step_pair touched, for the work counters: blocks
+ * loaded for J alone, and the distinct 128-byte lines its bounds fall in
+ * with this layout (256 rows a line) and with a 64-byte block of 192 rows
+ * (384 rows a line). */
+struct GsStepTouch {
+    int jblocks, lines256, lines384;
+};
 
 /* One backward step with base c of an interval I = [l,u] (only when doI)
  * and of a sub-interval J = [jl,ju] of it (jl > ju: none; left unchanged).  J's
  * bounds lie between I's, so their blocks are loaded only where they differ
  * from the blocks of I's bounds, and all loads are issued before any is
- * used.  Returns the number of 32-byte blocks loaded (0..4). */
+ * used.  Returns the number of 32-byte blocks loaded (0..4); jblocks gets
+ * the number loaded for J alone. */
 __device__ __forceinline__ int gs_step_pair(const GsDevIndex &I, uint32_t &l, uint32_t &u,
-                                            uint32_t &jl, uint32_t &ju, uint32_t c, bool doI)
+                                            uint32_t &jl, uint32_t &ju, uint32_t c, bool doI,
+                                            GsStepTouch &touch)
 {
     const uint32_t P = I.primary;
     const bool lz = (l == 0), uf = (u == I.seq_len);
@@ -194,7 +227,18 @@ __device__ __forceinline__ int gs_step_pair(const GsDevIndex &I, uint32_t &l, ui
         l = base + ol + 1u;
         u = base + ou;
     }
+    const bool vu = doI && !uf, vl = doI && !lz, vju = jn && !juf, vjl = jn && !jlz;
+    touch.jblocks = (int)n2 + (int)n3;
+    touch.lines256 = gs_distinct4(ua >> 8, vu, la >> 8, vl, jua >> 8, vju, jla >> 8, vjl);
+    touch.lines384 = gs_distinct4(ua / 384u, vu, la / 384u, vl, jua / 384u, vju, jla / 384u, vjl);
     return (int)n0 + (int)n1 + (int)n2 + (int)n3;
+}
+
+__device__ __forceinline__ int gs_step_pair(const GsDevIndex &I, uint32_t &l, uint32_t &u,
+                                            uint32_t &jl, uint32_t &ju, uint32_t c, bool doI)
+{
+    GsStepTouch t;
+    return gs_step_pair(I, l, u, jl, ju, c, doI, t);
 }
 
 /* LF of a BWT row (bwt_inv_psi_gpu, seed_gen.cu:455-484).  lf_mode
@@ -206,9 +250,7 @@ __device__ __forceinline__ uint32_t gs_lf(const GsDevIndex &I, uint32_t k, int l
     uint32_t ka = k - ((k > I.primary) ? 1u : 0u);
     if (lf_mode == GS_LF_GPUSEED && ka == I.primary) return 0;
     GsBlk B = gs_load_block(I.occ, ka >> 6);
-    uint32_t kw = (ka >> 4) & 3u;
-    uint32_t word = gs_sel4(kw, B.w[4], B.w[5], B.w[6], B.w[7]);
-    uint32_t c = (word >> ((~ka & 15u) << 1)) & 3u;
+    uint32_t c = gs_block_base(B, ka);
     return gs_L2(I, c) + gs_occ_in_block(B, ka, c);
 }
 

@@ -71,8 +71,7 @@ __global__ void gs_text_chain_kernel(GsDevIndex I, uint32_t *saf, uint8_t *t8, u
             }
             const uint32_t ka = row - (row > I.primary ? 1u : 0u);
             const GsBlk B = gs_load_block(I.occ, ka >> 6);
-            const uint32_t word = gs_sel4((ka >> 4) & 3u, B.w[4], B.w[5], B.w[6], B.w[7]);
-            const uint32_t c = (word >> ((~ka & 15u) << 1)) & 3u;
+            const uint32_t c = gs_block_base(B, ka);
             t8[s - 1] = (uint8_t)c;
             row = gs_L2(I, c) + gs_occ_in_block(B, ka, c);
             s--;
@@ -165,6 +164,34 @@ int gs_build_text(GsDevIndex &I, uint32_t *saf, uint32_t *text, uint32_t *isa, c
 
 /* Longer start table by reference length: one table entry per distinct
  * kx-mer the text can hold (4^kx around seq_len) */
+/* the 16 high (hi) or low bits of a word of 16 two-bit bases, first base
+ * (bits 30-31) at bit 15 */
+__device__ __forceinline__ uint32_t gs_slice16(uint32_t w, bool hi)
+{
+    uint32_t x = (hi ? w >> 1 : w) & 0x55555555u;
+    x = (x | (x >> 1)) & 0x33333333u;
+    x = (x | (x >> 2)) & 0x0f0f0f0fu;
+    x = (x | (x >> 4)) & 0x00ff00ffu;
+    return (x | (x >> 8)) & 0x0000ffffu;
+}
+
+/* The file's base words of each block (16 two-bit bases per word, first
+ * base in the top bits, seed_gen.cu:52-58) become the bit-sliced words the
+ * kernels read (gs_fm.cuh): H0, H1 = high bits of bases 0-31, 32-63, L0, L1
+ * = low bits, base i at bit 31 - (i & 31).  The counts stay. */
+__global__ void gs_bitslice_kernel(uint32_t *occ, uint64_t nblk)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nblk; b += stride) {
+        uint32_t *p = occ + b * GS_BLOCK_WORDS + 4;
+        const uint32_t w0 = p[0], w1 = p[1], w2 = p[2], w3 = p[3];
+        p[0] = (gs_slice16(w0, true) << 16) | gs_slice16(w1, true);
+        p[1] = (gs_slice16(w2, true) << 16) | gs_slice16(w3, true);
+        p[2] = (gs_slice16(w0, false) << 16) | gs_slice16(w1, false);
+        p[3] = (gs_slice16(w2, false) << 16) | gs_slice16(w3, false);
+    }
+}
+
 static int auto_kmer_len(uint32_t seq_len)
 {
     if (seq_len > (1u << 30)) return 16;
@@ -233,6 +260,11 @@ static int upload(uint32_t primary, const uint32_t L2_1to4[4], const uint32_t *b
         (e = cudaMemcpy(idx->d_occ, bwt, copy_words * 4, cudaMemcpyHostToDevice)) != cudaSuccess) {
         gs_index_free(idx);
         return gs_cuda_fail(e, "index upload");
+    }
+    gs_bitslice_kernel<<<152 * 8, 256>>>(idx->d_occ, nblk);
+    if ((e = cudaGetLastError()) != cudaSuccess) {
+        gs_index_free(idx);
+        return gs_cuda_fail(e, "occurrence table layout");
     }
     uint32_t minus1 = 0xffffffffu;
     if ((e = cudaMemcpy(idx->d_sa, &minus1, 4, cudaMemcpyHostToDevice)) != cudaSuccess ||

@@ -11,7 +11,7 @@
 #include "../../include/gpuseed.h"
 
 #define GS_OCC_INTERVAL 64u   /* rows per occurrence block (seed_gen.cu:29) */
-#define GS_BLOCK_WORDS 8u     /* 4 counts + 4 two-bit BWT words = 32 bytes */
+#define GS_BLOCK_WORDS 8u     /* 4 counts + 4 bit-slice words of 64 bases = 32 bytes */
 #define GS_K0 13              /* k-mer table length (seed_gen.cu:2822) */
 #define GS_HIST 8             /* containment history depth of the batched search */
 #define GS_CHUNK 31           /* candidates owned by one warp work item */
@@ -21,7 +21,9 @@
 
 /* Device view of the index, passed by value to every kernel.
  * occ: one 32-byte block per 64 rows of the $-removed BWT string:
- *      {count of A, C, G, T before the block, 4 words of 16 bases, MSB first}.
+ *      {count of A, C, G, T before the block, H0, H1, L0, L1}: the high and
+ *      low bits of the block's 64 bases, base i at bit 31 - (i & 31) of
+ *      word i >> 5 (gs_fm.cuh).
  * sa:  sampled suffix array, sa[0] = 0xffffffff (the $ row).
  * kmer: (l,u) of every 13-mer, base j at bits 2j, processed first.
  * Optional text structures, all built from occ and sa in HBM:

@@ -693,11 +693,17 @@ __device__ __forceinline__ bool gs_text_round(const GsDevIndex &I, const unsigne
  * Returns false when the walk is over (killed: it ended by containment).
  * A step that leaves the walker eligible for text mode sets jl to
  * GS_TEXT_MARK. */
+/* walk-pass counters of a count_work pass (gs_ctx_last_walk_counts) */
+struct GsWalkCounts {
+    unsigned long long steps, jsteps, jblocks, jshrank, jwalkers, lines256, lines384;
+};
+
 template <int NSTOP, int COUNT, bool TEXT>
 __device__ __forceinline__ bool gs_walk_step(const GsDevIndex &I, const unsigned char *seq, int iL,
                                              bool fwd, int dir, uint32_t &l, uint32_t &u,
                                              uint32_t &jl, uint32_t &ju, int &pos, bool &jpend,
-                                             bool &killed, unsigned long long &wb)
+                                             bool &killed, unsigned long long &wb,
+                                             GsWalkCounts *wc = nullptr)
 {
     /* TEXT: text-mode states run here; otherwise the caller hands a walker
      * that enters text mode to the text pass */
@@ -726,8 +732,20 @@ __device__ __forceinline__ bool gs_walk_step(const GsDevIndex &I, const unsigned
         /* settle over a wildcard: J unchanged */
     } else {
         uint32_t nl = l, nu = u;
-        int blocks = gs_step_pair(I, nl, nu, jl, ju, c, !settle);
+        const bool had_j = jl <= ju;
+        GsStepTouch touch;
+        int blocks = gs_step_pair(I, nl, nu, jl, ju, c, !settle, touch);
         if (COUNT) wb += (unsigned long long)blocks;
+        if (COUNT && wc) {
+            wc->steps++;
+            wc->lines256 += (unsigned long long)touch.lines256;
+            wc->lines384 += (unsigned long long)touch.lines384;
+            if (had_j) {
+                wc->jsteps++;
+                wc->jblocks += (unsigned long long)touch.jblocks;
+                if (!settle && nl <= nu && nu - nl < u - l) wc->jshrank++;
+            }
+        }
         if (text) {
             l = nl;
             u = nu;
@@ -934,6 +952,7 @@ __global__ void __launch_bounds__(128, 8) gs_search_walk(GsDevIndex I, GsBatch B
     int anchor = 0, pos = 0, iL = 0, dir = 0;
     bool fwd = false;
     const unsigned char *seq = NULL;
+    GsWalkCounts wc = {0ull, 0ull, 0ull, 0ull, 0ull, 0ull, 0ull};
     for (;;) {
         uint32_t need = __ballot_sync(0xffffffffu, !have);
         while (need && !exhausted) {
@@ -970,6 +989,7 @@ __global__ void __launch_bounds__(128, 8) gs_search_walk(GsDevIndex I, GsBatch B
                     have = true;
                     killed = false;
                     jpend = (w.anchor & GS_WALKER_JPEND) != 0;
+                    if (COUNT && (jpend || jl <= ju)) wc.jwalkers++;
                 }
             }
             win += take;
@@ -980,7 +1000,7 @@ __global__ void __launch_bounds__(128, 8) gs_search_walk(GsDevIndex I, GsBatch B
             continue;
         }
         if (have && !gs_walk_step<NSTOP, COUNT, false>(I, seq, iL, fwd, dir, l, u, jl, ju, pos,
-                                                       jpend, killed, wb)) {
+                                                       jpend, killed, wb, &wc)) {
             gs_write_record(B, r, n, fwd, anchor, pos, l, u, true, killed);
             have = false;
         }
@@ -1013,7 +1033,15 @@ __global__ void __launch_bounds__(128, 8) gs_search_walk(GsDevIndex I, GsBatch B
             }
         }
     }
-    if (COUNT) gs_add_work(B, 0, wb);
+    if (COUNT) {
+        gs_add_work(B, 0, wb);
+        unsigned long long v[7] = {wc.steps, wc.jsteps, wc.jblocks, wc.jshrank, wc.jwalkers,
+                                   wc.lines256, wc.lines384};
+        for (int i = 0; i < 7; i++) {
+            for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+            if (lane == 0) atomicAdd(&B.work[4 + i], v[i]);
+        }
+    }
 }
 
 /* Text pass: the walkers the walk pass handed over, one per thread, each

@@ -297,11 +297,24 @@ extern "C" int gs_server_submit(gs_server *s, const char *seqs, const uint64_t *
     r->seqs.resize(bytes);
     r->offs.resize(n_reads);
     r->lens.assign(lengths, lengths + n_reads);
+    /* reads that lie back to back in the caller's buffer (the usual case)
+     * are copied in one piece; otherwise read by read */
+    bool packed = true;
+    for (uint32_t i = 0; i + 1 < n_reads && packed; i++)
+        packed = offsets[i + 1] == offsets[i] + lengths[i];
     uint64_t w = 0;
-    for (uint32_t i = 0; i < n_reads; i++) {
-        memcpy(r->seqs.data() + w, seqs + offsets[i], lengths[i]);
-        r->offs[i] = w;
-        w += lengths[i];
+    if (packed && n_reads) {
+        memcpy(r->seqs.data(), seqs + offsets[0], bytes);
+        for (uint32_t i = 0; i < n_reads; i++) {
+            r->offs[i] = w;
+            w += lengths[i];
+        }
+    } else {
+        for (uint32_t i = 0; i < n_reads; i++) {
+            memcpy(r->seqs.data() + w, seqs + offsets[i], lengths[i]);
+            r->offs[i] = w;
+            w += lengths[i];
+        }
     }
     r->bases = bytes;
     r->est_bytes = estimate_bytes(bytes, n_reads);

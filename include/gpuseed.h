@@ -236,6 +236,15 @@ int gs_ctx_last_timing(gs_ctx *ctx, float *search_ms, float *total_ms);
  * they are the lookups those kernels execute. */
 int gs_ctx_last_work(gs_ctx *ctx, uint64_t out[4]);
 
+/* Batched search, last pass run with count_work = 1 (one pass, not
+ * chunks): the walk pass's steps, its steps with a neighbour interval J, the
+ * 32-byte blocks it loaded for J alone (J's bounds outside the blocks of
+ * I's), the steps with J that shrank I, the walkers that started with J,
+ * and the distinct 128-byte lines its steps' bounds fall in -- with this
+ * occurrence table (256 rows a line) and as if blocks held 192 rows in 64
+ * bytes (384 rows a line).  No counterpart in the reference: these bound
+ * what another containment test or block size could save. */
+int gs_ctx_last_walk_counts(gs_ctx *ctx, uint64_t out[7]);
 /* Batched search (GS_KERNEL_BATCHED): candidates of the last call that the
  * start pass handed to the walk pass, and the walker buffer's capacity
  * (handed beyond it: walked in the start pass instead). */
