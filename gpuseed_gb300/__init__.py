@@ -123,6 +123,7 @@ def lib():
         L.gs_autotune.argtypes = [vp, vp, vp, vp, u32, C.POINTER(Params), u32, C.POINTER(C.c_float)]
         L.gs_server_start.argtypes = [vp, C.POINTER(ServerOpts), C.POINTER(vp)]
         L.gs_server_submit.argtypes = [vp, vp, vp, vp, u32, C.POINTER(u64)]
+        L.gs_server_submit_ref.argtypes = [vp, vp, vp, vp, u32, C.POINTER(u64)]
         L.gs_server_wait.argtypes = [vp, u64, i32]
         L.gs_server_result.argtypes = [vp, u64, C.POINTER(ResultView), C.POINTER(C.c_double)]
         L.gs_server_release.argtypes = [vp, u64]
@@ -382,15 +383,20 @@ class Server:
         h = C.c_void_p()
         check(lib().gs_server_start(index.h, C.byref(o), C.byref(h)))
         self.h = h
+        self._held = {}
 
-    def submit(self, seqs, offsets, lengths) -> int:
+    def submit(self, seqs, offsets, lengths, copy=True) -> int:
+        """copy=False: gs_server_submit_ref -- the bases are read in place,
+        and this object keeps the buffer alive until the request is released"""
         buf = np.frombuffer(seqs, dtype=np.uint8) if isinstance(seqs, (bytes, bytearray)) else \
             np.ascontiguousarray(seqs, dtype=np.uint8)
         offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
         lengths = np.ascontiguousarray(lengths, dtype=np.uint32)
         rid = C.c_uint64()
-        check(lib().gs_server_submit(self.h, _ptr(buf), _ptr(offsets), _ptr(lengths), lengths.size,
-                                     C.byref(rid)))
+        fn = lib().gs_server_submit if copy else lib().gs_server_submit_ref
+        check(fn(self.h, _ptr(buf), _ptr(offsets), _ptr(lengths), lengths.size, C.byref(rid)))
+        if not copy:
+            self._held[rid.value] = buf
         return rid.value
 
     def wait(self, rid: int, timeout_ms: int = -1) -> int:
@@ -403,6 +409,7 @@ class Server:
         res = Result(v)
         if release:
             lib().gs_server_release(self.h, rid)
+            self._held.pop(rid, None)
         return res, lat.value
 
     def replay(self, pool_seqs, pool_offsets, pool_lengths, first, count, gap_ms):

@@ -136,6 +136,16 @@ int gs_build_kmerx_table(const GsDevIndex &I, uint2 *table, int kx, cudaStream_t
     return GS_OK;
 }
 
+/* a start-table entry: one random 8-byte load whose L2 fill is 64 bytes
+ * (the default fills 128 for random loads; the table's lookups are bound by
+ * the DRAM access rate, and the start pass also streams the walker buffer) */
+__device__ __forceinline__ uint2 gs_ld_entry(const uint2 *p)
+{
+    uint2 v;
+    asm("ld.global.nc.L2::64B.v2.u32 {%0,%1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+}
+
 /* Start of a candidate: the interval of its first KT bases (forward: the
  * bases anchor, anchor-1, ...; reverse: the complement codes anchor,
  * anchor+1, ...; the first base at bits 0-1).  Returns false when one of the
@@ -173,14 +183,14 @@ __device__ __forceinline__ bool gs_start(const GsDevIndex &I, const unsigned cha
     w_kmer++;
     if (first_bad == KT) {
         if (KT == GS_K0) {
-            uint2 iv = __ldg(&I.kmer[pat]);
+            uint2 iv = gs_ld_entry(&I.kmer[pat]);
             l = iv.x;
             u = iv.y;
             pos = anchor + dir * (KT - 1);
             alive = l <= u;
             return true;
         }
-        uint2 iv = __ldg(&I.kmerx[pat]);
+        uint2 iv = gs_ld_entry(&I.kmerx[pat]);
         uint32_t code = iv.y & 7u, size = iv.y >> 3;
         if (code != 7u) {
             fcode = code;
@@ -199,7 +209,7 @@ __device__ __forceinline__ bool gs_start(const GsDevIndex &I, const unsigned cha
         }
         /* interval too wide to pack: the 13-mer start below */
     }
-    uint2 iv = __ldg(&I.kmer[pat & ((1u << (2 * GS_K0)) - 1u)]);
+    uint2 iv = gs_ld_entry(&I.kmer[pat & ((1u << (2 * GS_K0)) - 1u)]);
     l = iv.x;
     u = iv.y;
     alive = l <= u;

@@ -41,6 +41,7 @@ double now_ms()
 struct Req {
     uint64_t id;
     std::vector<char> seqs;
+    const char *ext;            /* gs_server_submit_ref: the caller's bases, in place */
     std::vector<uint64_t> offs;
     std::vector<uint32_t> lens;
     uint64_t bases;
@@ -175,7 +176,7 @@ static void worker_main(gs_server *s, int slot)
         if (rc == GS_OK)
             for (Req *r : batch) {
                 r->t_start = t0;
-                memcpy(seqs + wb, r->seqs.data(), r->bases);
+                memcpy(seqs + wb, r->ext ? r->ext : r->seqs.data(), r->bases);
                 for (size_t i = 0; i < r->lens.size(); i++) {
                     offs[wr] = wb + r->offs[i];
                     lens[wr] = r->lens[i];
@@ -218,6 +219,7 @@ static void worker_main(gs_server *s, int slot)
                 r->done = true;
                 r->t_done = t1;
                 r->seqs.clear();
+                r->ext = NULL;
                 if (rc == GS_OK) s->stats.completed++;
                 else s->stats.failed++;
             }
@@ -267,8 +269,8 @@ extern "C" int gs_server_start(gs_index *idx, const gs_server_opts *opts, gs_ser
     return GS_OK;
 }
 
-extern "C" int gs_server_submit(gs_server *s, const char *seqs, const uint64_t *offsets,
-                                const uint32_t *lengths, uint32_t n_reads, uint64_t *request_id)
+static int submit(gs_server *s, const char *seqs, const uint64_t *offsets,
+                  const uint32_t *lengths, uint32_t n_reads, uint64_t *request_id, bool by_ref)
 {
     if (!s || !request_id || (n_reads && (!seqs || !offsets || !lengths))) {
         gs_set_error("gs_server_submit: null argument");
@@ -294,7 +296,7 @@ extern "C" int gs_server_submit(gs_server *s, const char *seqs, const uint64_t *
     r->pos_off.clear();
     r->seeds.clear();
     r->pos.clear();
-    r->seqs.resize(bytes);
+    r->ext = NULL;
     r->offs.resize(n_reads);
     r->lens.assign(lengths, lengths + n_reads);
     /* reads that lie back to back in the caller's buffer (the usual case)
@@ -304,12 +306,21 @@ extern "C" int gs_server_submit(gs_server *s, const char *seqs, const uint64_t *
         packed = offsets[i + 1] == offsets[i] + lengths[i];
     uint64_t w = 0;
     if (packed && n_reads) {
-        memcpy(r->seqs.data(), seqs + offsets[0], bytes);
+        /* by reference: the worker copies the bases straight from the
+         * caller's buffer when it merges the pass */
+        if (by_ref) {
+            r->ext = seqs + offsets[0];
+            r->seqs.clear();
+        } else {
+            r->seqs.resize(bytes);
+            memcpy(r->seqs.data(), seqs + offsets[0], bytes);
+        }
         for (uint32_t i = 0; i < n_reads; i++) {
             r->offs[i] = w;
             w += lengths[i];
         }
     } else {
+        r->seqs.resize(bytes);
         for (uint32_t i = 0; i < n_reads; i++) {
             memcpy(r->seqs.data() + w, seqs + offsets[i], lengths[i]);
             r->offs[i] = w;
@@ -337,6 +348,19 @@ extern "C" int gs_server_submit(gs_server *s, const char *seqs, const uint64_t *
     }
     s->cv_work.notify_one();
     return GS_OK;
+}
+
+extern "C" int gs_server_submit(gs_server *s, const char *seqs, const uint64_t *offsets,
+                                const uint32_t *lengths, uint32_t n_reads, uint64_t *request_id)
+{
+    return submit(s, seqs, offsets, lengths, n_reads, request_id, false);
+}
+
+extern "C" int gs_server_submit_ref(gs_server *s, const char *seqs, const uint64_t *offsets,
+                                    const uint32_t *lengths, uint32_t n_reads,
+                                    uint64_t *request_id)
+{
+    return submit(s, seqs, offsets, lengths, n_reads, request_id, true);
 }
 
 extern "C" int gs_server_wait(gs_server *s, uint64_t id, int32_t timeout_ms)
@@ -463,7 +487,9 @@ extern "C" int gs_server_replay(gs_server *s, const char *pool_seqs, const uint6
         offs.resize(n);
         uint64_t base = pool_offsets[f];
         for (uint32_t j = 0; j < n; j++) offs[j] = pool_offsets[f + j] - base;
-        int rc = gs_server_submit(s, pool_seqs + base, offs.data(), pool_lengths + f, n, &ids[i]);
+        /* the pool outlives every request: submitted by reference */
+        int rc = gs_server_submit_ref(s, pool_seqs + base, offs.data(), pool_lengths + f, n,
+                                      &ids[i]);
         if (rc) return rc;
     }
     double t_sub = now_ms();

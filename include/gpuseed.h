@@ -294,6 +294,14 @@ int gs_server_start(gs_index *idx, const gs_server_opts *opts, gs_server **out);
 /* Copies the request's reads; the caller's buffers are free on return. */
 int gs_server_submit(gs_server *srv, const char *seqs, const uint64_t *offsets,
                      const uint32_t *lengths, uint32_t n_reads, uint64_t *request_id);
+/* The same without copying the bases when the reads lie back to back in
+ * seqs (offsets[i+1] == offsets[i] + lengths[i]): the pass reads them from
+ * the caller's buffer, which must stay unchanged until gs_server_wait
+ * reports the request done.  Offsets and lengths are still copied; reads
+ * that are not back to back are copied as by gs_server_submit.  For a
+ * client that submits faster than one thread copies bases. */
+int gs_server_submit_ref(gs_server *srv, const char *seqs, const uint64_t *offsets,
+                         const uint32_t *lengths, uint32_t n_reads, uint64_t *request_id);
 /* 0 when done (or the request's error), GS_ETIMEOUT after timeout_ms (< 0: wait). */
 int gs_server_wait(gs_server *srv, uint64_t request_id, int32_t timeout_ms);
 /* Host view of a finished request's seeds (valid until release) and its

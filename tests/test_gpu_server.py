@@ -70,3 +70,30 @@ def test_admission_refuses_what_cannot_fit(env):
     assert srv.wait(small, 60_000) == 0
     assert srv.wait(big, 60_000) == -4      # GS_ENOMEM: larger than the whole budget
     srv.stop()
+
+
+def test_submit_by_reference(env):
+    """gs_server_submit_ref: reads back to back in the caller's buffer are
+    read in place, others are copied; either way each request's seeds equal
+    a direct pass over its reads."""
+    import gpuseed_gb300 as gs
+    reqs = _requests(env["codes"], 30, seed=8)
+    srv = gs.Server(env["idx"], n_slots=2, k=19, smem=True)
+    try:
+        ids = []
+        for i, reads in enumerate(reqs):
+            seqs, offs, lens = pack(reads)
+            if i % 3 == 2 and lens.size > 1:
+                # not back to back: a gap of 7 bytes before every read
+                buf = b"".join(b"NNNNNNN" + r for r in reads)
+                offs = (np.cumsum(np.concatenate([[0], lens[:-1] + 7])) + 7).astype(np.uint64)
+                seqs = buf
+            ids.append(srv.submit(seqs, offs, lens, copy=False))
+        for reads, rid in zip(reqs, ids):
+            assert srv.wait(rid) == 0
+            got, _ = srv.result(rid)
+            want = env["ctx"].seed(*pack(reads), k=19, smem=True)
+            assert np.array_equal(got.seeds, want.seeds) and np.array_equal(got.pos, want.pos)
+            assert np.array_equal(got.read_seed_off, want.read_seed_off)
+    finally:
+        srv.stop()
