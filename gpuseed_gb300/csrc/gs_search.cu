@@ -552,7 +552,7 @@ __global__ void __launch_bounds__(256, 5) gs_search_lockstep(GsDevIndex I, GsBat
 #define GS_WALKER_JPEND 0x40000000u   /* anchor flag: J is one base short of I's far end */
 #define GS_WALKER_FWD 0x80000000u
 #define GS_WALKER_CHUNK 512u      /* buffer entries a warp reserves at a time */
-#define GS_WALK_WINDOW 256u       /* buffer entries a walk-pass warp takes at a time */
+#define GS_WALK_WINDOW 512u       /* buffer entries a walk-pass warp takes at a time */
 
 /* Text mode.  A walker whose interval is one row [l,l] and whose J is
  * empty can no longer be contained: its walk only extends one occurrence,
