@@ -504,7 +504,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     GS_CUDA(cudaMemsetAsync(c->queue, 0, 32, st));
     B.slot_off = c->slot_cnt;
     B.item_off = c->item_cnt;
-    RC(gs_launch_prepare(B, st));
+    RC(gs_launch_prepare(I, B, p->kernel, st));
     RC(exclusive_scan(c, c->slot_cnt, c->slot_off, nr1));
     RC(exclusive_scan(c, c->item_cnt, c->item_off, nr1));
     B.slot_off = c->slot_off;
@@ -542,12 +542,14 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     c->last_walker_cap = 0;
     c->last_text_cap = 0;
     if (p->kernel == GS_KERNEL_BATCHED && p->walker_slots >= 0) {
-        /* entries per 16 work items: as asked, or automatic -- 16 per item
+        /* entries per 16 work items of 31 candidates (a paired item of 30
+         * windows counts as two): as asked, or automatic -- 16 per item
          * with a start table (forced codes settle most candidates), all 31
          * without, and 1.5x more after a pass that filled its buffer */
         if (!c->walker_per16) c->walker_per16 = I.kx > GS_K0 ? 256u : 512u;
         const uint64_t per16 = p->walker_slots ? (uint64_t)p->walker_slots : c->walker_per16;
-        uint64_t want = ((uint64_t)n_items * per16 + 15u) / 16u + 32u;
+        const uint64_t units = (uint64_t)n_items * (B.paired ? 2u : 1u);
+        uint64_t want = (units * per16 + 15u) / 16u + 32u;
         if (want > (1ull << 31)) want = 1ull << 31;   /* 32-bit buffer counter */
         RC(grow(c->walkers, c->cap_walkers, (size_t)want, c->st));
         B.walkers = c->walkers;
@@ -557,7 +559,7 @@ static int run_pipeline(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
          * what reads with a few differences per 100 bases need; without
          * room a walker walks on in the walk pass */
         if (I.text_min) {
-            uint64_t tw = (uint64_t)n_items * 2u + 64u;
+            uint64_t tw = units * 2u + 64u;
             if (tw > (1ull << 31)) tw = 1ull << 31;
             RC(grow(c->text_jobs, c->cap_text_jobs, (size_t)tw, c->st));
             B.text_jobs = c->text_jobs;
@@ -736,7 +738,7 @@ static int enqueue_pass(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     GS_CUDA(cudaMemsetAsync(c->queue, 0, 32, st));
     B.slot_off = c->slot_cnt;
     B.item_off = c->item_cnt;
-    RC(gs_launch_prepare(B, st));
+    RC(gs_launch_prepare(I, B, GS_KERNEL_BATCHED, st));
     RC(exclusive_scan(c, c->slot_cnt, c->slot_off, nr1));
     RC(exclusive_scan(c, c->item_cnt, c->item_off, nr1));
     B.slot_off = c->slot_off;

@@ -21,7 +21,7 @@ struct gs_index {
     uint32_t *d_occ;
     uint32_t *d_sa;
     uint2 *d_kmer;
-    uint2 *d_kmerx;
+    uint4 *d_kmerx;
     uint32_t *d_saf, *d_text, *d_isa;
     size_t occ_bytes, sa_bytes, kmer_bytes, kmerx_bytes, text_bytes;
     float l2_hit_ratio;
@@ -534,8 +534,8 @@ extern "C" int gs_index_set_kmer_len(gs_index *idx, int kx)
     idx->dev.kmerx = NULL;
     idx->dev.kx = 0;
     if (kx == GS_K0) return GS_OK;
-    size_t bytes = (size_t)8 << (2 * kx);
-    uint2 *t = NULL;
+    size_t bytes = (size_t)16 << (2 * kx);
+    uint4 *t = NULL;
     cudaError_t e = cudaMalloc(&t, bytes);
     if (e != cudaSuccess) return gs_cuda_fail(e, "cudaMalloc(k-mer start table)");
     int rc = gs_build_kmerx_table(idx->dev, t, kx, 0);

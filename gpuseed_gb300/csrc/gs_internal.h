@@ -15,6 +15,7 @@
 #define GS_K0 13              /* k-mer table length (seed_gen.cu:2822) */
 #define GS_HIST 8             /* containment history depth of the batched search */
 #define GS_CHUNK 31           /* candidates owned by one warp work item */
+#define GS_PCHUNK 30          /* read positions owned by one paired work item */
 #define GS_HANDOFF_LANES 2    /* default hand-over threshold of the batched search */
 #define GS_HANDOFF_STEPS 4
 #define GS_QUEUE_CHUNK 4      /* default work items per queue grab */
@@ -46,7 +47,8 @@ struct GsDevIndex {
     const uint32_t *occ;
     const uint32_t *sa;
     const uint2 *kmer;
-    const uint2 *kmerx;        /* optional (l,u) table of all kx-mers, same bit order */
+    const uint4 *kmerx;        /* optional table of all kx-mers, same bit order: x,y the
+                                * packed entry of X, z,w that of X's reverse complement */
     const uint32_t *saf;
     const uint32_t *text;
     const uint32_t *isa;
@@ -115,6 +117,9 @@ struct GsBatch {
     int32_t handoff_steps;     /* ... after at least this many lockstep steps */
     uint32_t max_occ;          /* 0 or the largest interval an output seed may have */
     int32_t mem_next;          /* GS_MEM_NEXT_READ | GS_MEM_NEXT_GPUSEED (MEM mode) */
+    int32_t paired;            /* batched start pass: work items of read positions, one
+                                * table entry for both strands' candidates (set by
+                                * gs_launch_prepare) */
     GsWalker *walkers;         /* batched search: survivors of the start pass */
     uint64_t walker_cap;       /* entries allocated (0: every walk stays in the start pass) */
     struct GsTextJob *text_jobs;   /* walkers handed to the text pass */
@@ -195,7 +200,7 @@ struct GsDeviceGuard {
 int gs_build_kmer_table(const GsDevIndex &idx, uint2 *table, cudaStream_t st);
 int gs_launch_text_lengths(const GsTextArgs &a, cudaStream_t st);
 int gs_launch_text_write(const GsTextArgs &a, cudaStream_t st);
-int gs_build_kmerx_table(const GsDevIndex &idx, uint2 *table, int kx, cudaStream_t st);
+int gs_build_kmerx_table(const GsDevIndex &idx, uint4 *table, int kx, cudaStream_t st);
 /* full SA, text and sampled ISA from occ + sa; GS_EFORMAT when the index
  * does not describe one text (the structures are then not used) */
 int gs_build_text(GsDevIndex &idx, uint32_t *saf, uint32_t *text, uint32_t *isa, cudaStream_t st);
@@ -203,7 +208,7 @@ int gs_build_text(GsDevIndex &idx, uint32_t *saf, uint32_t *text, uint32_t *isa,
  * the kernels read the count from item_off[n_reads] on the device */
 int gs_launch_search(const GsDevIndex &idx, GsBatch &b, int kernel, int queue_chunk,
                      int ctas_per_sm, uint32_t n_items, cudaStream_t st);
-int gs_launch_prepare(GsBatch &b, cudaStream_t st);
+int gs_launch_prepare(const GsDevIndex &I, GsBatch &b, int kernel, cudaStream_t st);
 int gs_launch_finalize_count(const GsDevIndex &idx, GsBatch &b, cudaStream_t st);
 int gs_launch_finalize_emit(const GsDevIndex &idx, GsBatch &b, cudaStream_t st);
 /* n_seeds / n_pos: host-known totals, or 0 to size the grids by the

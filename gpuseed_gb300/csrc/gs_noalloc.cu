@@ -160,7 +160,7 @@ extern "C" int gs_seed_noalloc(gs_index *idx, const char *d_seqs, const uint64_t
     /* slots and work items per read */
     B.slot_off = slot_cnt;
     B.item_off = item_cnt;
-    NA_RC(gs_launch_prepare(B, st));
+    NA_RC(gs_launch_prepare(I, B, GS_KERNEL_LOCKSTEP, st));
     GS_CUDA(cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, slot_cnt, slot_off, (int64_t)nr1, st));
     GS_CUDA(cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, item_cnt, item_off, (int64_t)nr1, st));
     uint64_t n_slots = 0;

@@ -53,7 +53,7 @@ int gs_build_kmer_table(const GsDevIndex &I, uint2 *table, cudaStream_t st)
     return GS_OK;
 }
 
-/* Longer start table, built in three passes over all kx-mers (base j at
+/* Longer start table, built in four passes over all kx-mers (base j at
  * bits 2j, processed first, i.e. the string's last character sits at bits
  * 0-1):
  *   1. (l,u) from the 13-mer prefix interval plus kx-13 steps;
@@ -62,34 +62,49 @@ int gs_build_kmer_table(const GsDevIndex &I, uint2 *table, cudaStream_t st)
  *      first character from the kx-mer table entry of (X without its first
  *      character)·c;
  *   3. packing: entry.x = l, entry.y = size << 3 | code, code 0-3 the forced
- *      base, 4 none, 7 "size does not fit 29 bits: start from the 13-mer".
+ *      base, 4 none, 7 "size does not fit 29 bits: start from the 13-mer";
+ *   4. entry.z, entry.w = the packed entry of gs_kmer_rc(X), the kx-mer of
+ *      X's reverse complement in the same bit order.
  * A candidate whose kx-mer is always followed by its neighbour's next base is
  * contained in that neighbour (see the file comment) and needs no walk;
- * gs_search_plain stops such candidates at their start. */
-__global__ void gs_kmerx_kernel(GsDevIndex I, uint2 *table, int kx, uint64_t n)
+ * gs_search_plain stops such candidates at their start.  A read's window
+ * R[s..s+kx-1] is the start string of its forward candidate ending at
+ * s+kx-1 and, as complement codes, of its reverse candidate starting at s:
+ * the two keys are X and gs_kmer_rc(X), so one 16-byte entry starts both. */
+__device__ __forceinline__ uint32_t gs_kmer_rc(uint32_t X, int kx)
+{
+    /* complement every base (3 - c = c ^ 3), then reverse the order of the
+     * kx 2-bit groups */
+    const uint32_t b = __brev(~X);
+    return (((b >> 1) & 0x55555555u) | ((b & 0x55555555u) << 1)) >> (32 - 2 * kx);
+}
+
+__global__ void gs_kmerx_kernel(GsDevIndex I, uint4 *table, int kx, uint64_t n)
 {
     for (uint64_t patt = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; patt < n;
          patt += (uint64_t)gridDim.x * blockDim.x) {
         uint2 iv = __ldg(&I.kmer[patt & ((1u << (2 * GS_K0)) - 1u)]);
         uint32_t l = iv.x, u = iv.y;
         for (int i = GS_K0; i < kx && l <= u; i++) gs_step(I, l, u, (uint32_t)(patt >> (i << 1)) & 3u);
-        table[patt] = make_uint2(l, u);
+        table[patt] = make_uint4(l, u, 0u, 0u);
     }
 }
 
-__global__ void gs_kmerx_code_kernel(GsDevIndex I, const uint2 *table, int kx, uint64_t n,
+__global__ void gs_kmerx_code_kernel(GsDevIndex I, const uint4 *table, int kx, uint64_t n,
                                      uint8_t *code)
 {
     const uint64_t mask = n - 1;
     for (uint64_t X = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; X < n;
          X += (uint64_t)gridDim.x * blockDim.x) {
-        uint2 e = table[X];
+        const uint4 e4 = table[X];
+        const uint2 e = make_uint2(e4.x, e4.y);
         uint8_t out = 4;
         if (e.x <= e.y) {
             uint32_t size = e.y - e.x + 1u;
             uint32_t first = (uint32_t)(X >> (2 * (kx - 1))) & 3u;   /* X's first character */
             for (uint32_t c = 0; c < 4; c++) {
-                uint2 y = table[((X << 2) | c) & mask];
+                const uint4 y4 = table[((X << 2) | c) & mask];
+                const uint2 y = make_uint2(y4.x, y4.y);
                 if (y.x > y.y) continue;
                 uint32_t l = y.x, u = y.y;
                 gs_step(I, l, u, first);
@@ -103,22 +118,34 @@ __global__ void gs_kmerx_code_kernel(GsDevIndex I, const uint2 *table, int kx, u
     }
 }
 
-__global__ void gs_kmerx_pack_kernel(uint2 *table, uint64_t n, const uint8_t *code)
+__global__ void gs_kmerx_pack_kernel(uint4 *table, uint64_t n, const uint8_t *code)
 {
     for (uint64_t X = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; X < n;
          X += (uint64_t)gridDim.x * blockDim.x) {
-        uint2 e = table[X];
+        const uint4 e = table[X];
         uint32_t size = e.x <= e.y ? e.y - e.x + 1u : 0u;
         uint32_t c = code[X];
         if (size >= (1u << 29)) {
             size = 0;
             c = 7;
         }
-        table[X] = make_uint2(e.x, (size << 3) | c);
+        table[X] = make_uint4(e.x, (size << 3) | c, 0u, 0u);
     }
 }
 
-int gs_build_kmerx_table(const GsDevIndex &I, uint2 *table, int kx, cudaStream_t st)
+/* pass 4: each entry's second half from the packed first half of its
+ * reverse complement's entry (reads only x,y and writes only z,w) */
+__global__ void gs_kmerx_pair_kernel(uint4 *table, int kx, uint64_t n)
+{
+    uint2 *w = reinterpret_cast<uint2 *>(table);
+    for (uint64_t X = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; X < n;
+         X += (uint64_t)gridDim.x * blockDim.x) {
+        const uint2 rc = w[2 * (uint64_t)gs_kmer_rc((uint32_t)X, kx)];
+        w[2 * X + 1] = rc;
+    }
+}
+
+int gs_build_kmerx_table(const GsDevIndex &I, uint4 *table, int kx, cudaStream_t st)
 {
     uint64_t n = 1ull << (2 * kx);
     gs_kmerx_kernel<<<152 * 64, 256, 0, st>>>(I, table, kx, n);
@@ -129,6 +156,10 @@ int gs_build_kmerx_table(const GsDevIndex &I, uint2 *table, int kx, cudaStream_t
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) {
         gs_kmerx_pack_kernel<<<152 * 64, 256, 0, st>>>(table, n, code);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        gs_kmerx_pair_kernel<<<152 * 64, 256, 0, st>>>(table, kx, n);
         e = cudaGetLastError();
     }
     cudaFreeAsync(code, st);
@@ -144,6 +175,52 @@ __device__ __forceinline__ uint2 gs_ld_entry(const uint2 *p)
     uint2 v;
     asm("ld.global.nc.L2::64B.v2.u32 {%0,%1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
     return v;
+}
+
+/* both halves of a paired start-table entry: one 16-byte load, the same
+ * 64-byte L2 fill */
+__device__ __forceinline__ uint4 gs_ld_pair(const uint4 *p)
+{
+    uint4 v;
+    asm("ld.global.nc.L2::64B.v4.u32 {%0,%1,%2,%3}, [%4];"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+        : "l"(p));
+    return v;
+}
+
+/* The start from the 13-mer table: the interval of the first 13 bases,
+ * then steps up to KT bases (a non-ACGT base is a wildcard, or stops the
+ * start under GS_N_STOP) */
+template <int NSTOP>
+__device__ __forceinline__ void gs_start_from13(const GsDevIndex &I, const unsigned char *seq,
+                                                int anchor, int dir, bool fwd, int KT, uint32_t pat,
+                                                uint32_t &l, uint32_t &u, int &pos, bool &alive,
+                                                unsigned long long &w_blk)
+{
+    uint2 iv = gs_ld_entry(&I.kmer[pat & ((1u << (2 * GS_K0)) - 1u)]);
+    l = iv.x;
+    u = iv.y;
+    alive = l <= u;
+    pos = anchor + dir * (GS_K0 - 1);
+    for (int j = GS_K0; j < KT && alive; j++) {
+        int np = pos + dir;
+        unsigned char ch = seq[np];
+        uint32_t c = fwd ? gs_fwd_code(ch) : gs_comp_code(ch);
+        if (c > 3u) {
+            if (NSTOP) alive = false;
+            else pos = np;
+        } else {
+            uint32_t nl = l, nu = u;
+            w_blk += (unsigned long long)gs_step(I, nl, nu, c);
+            if (nl > nu) {
+                alive = false;
+            } else {
+                l = nl;
+                u = nu;
+                pos = np;
+            }
+        }
+    }
 }
 
 /* Start of a candidate: the interval of its first KT bases (forward: the
@@ -190,7 +267,7 @@ __device__ __forceinline__ bool gs_start(const GsDevIndex &I, const unsigned cha
             alive = l <= u;
             return true;
         }
-        uint2 iv = gs_ld_entry(&I.kmerx[pat]);
+        uint2 iv = gs_ld_entry(reinterpret_cast<const uint2 *>(&I.kmerx[pat]));
         uint32_t code = iv.y & 7u, size = iv.y >> 3;
         if (code != 7u) {
             fcode = code;
@@ -209,29 +286,7 @@ __device__ __forceinline__ bool gs_start(const GsDevIndex &I, const unsigned cha
         }
         /* interval too wide to pack: the 13-mer start below */
     }
-    uint2 iv = gs_ld_entry(&I.kmer[pat & ((1u << (2 * GS_K0)) - 1u)]);
-    l = iv.x;
-    u = iv.y;
-    alive = l <= u;
-    for (int j = GS_K0; j < KT && alive; j++) {
-        int np = pos + dir;
-        unsigned char ch = seq[np];
-        uint32_t c = fwd ? gs_fwd_code(ch) : gs_comp_code(ch);
-        if (c > 3u) {
-            if (NSTOP) alive = false;
-            else pos = np;
-        } else {
-            uint32_t nl = l, nu = u;
-            w_blk += (unsigned long long)gs_step(I, nl, nu, c);
-            if (nl > nu) {
-                alive = false;
-            } else {
-                l = nl;
-                u = nu;
-                pos = np;
-            }
-        }
-    }
+    gs_start_from13<NSTOP>(I, seq, anchor, dir, fwd, KT, pat, l, u, pos, alive, w_blk);
     return true;
 }
 
@@ -241,10 +296,112 @@ __device__ __forceinline__ int gs_start_len(const GsDevIndex &I, int k)
     return (I.kx > GS_K0 && k > I.kx) ? I.kx : GS_K0;
 }
 
+static inline int gs_start_len_host(const GsDevIndex &I, int k)
+{
+    return (I.kx > GS_K0 && k > I.kx) ? I.kx : GS_K0;
+}
+
+/* one candidate's start as gs_start reports it */
+struct GsStart {
+    uint32_t l, u, fcode;
+    int pos;
+    bool ok, alive;
+};
+
+/* a start from one packed half of a start-table entry; false for code 7
+ * (interval too wide to pack: the caller starts from the 13-mer) */
+__device__ __forceinline__ bool gs_entry_start(uint32_t x, uint32_t y, int anchor, int dir, int KT,
+                                               GsStart &S)
+{
+    const uint32_t code = y & 7u, size = y >> 3;
+    if (code == 7u) return false;
+    S.fcode = code;
+    S.l = x;
+    S.u = size ? x + size - 1u : x - 1u;
+    S.pos = anchor + dir * (KT - 1);
+    S.alive = size != 0;
+    return true;
+}
+
+/* gs_start of one candidate: the rare starts of a paired window (a
+ * non-ACGT base in it, or an interval too wide to pack) */
+template <int NSTOP>
+__device__ __forceinline__ GsStart gs_start_apart(const GsDevIndex &I, const unsigned char *seq,
+                                               int anchor, bool fwd, int KT, int iL)
+{
+    GsStart S;
+    bool contained;
+    unsigned long long w_kmer = 0, w_blk = 0;
+    S.ok = gs_start<NSTOP, false>(I, seq, anchor, fwd ? -1 : 1, fwd, KT, iL, S.l, S.u, S.pos,
+                                  S.alive, contained, S.fcode, w_kmer, w_blk);
+    return S;
+}
+
+/* Both candidates of read window R[s..s+KT-1] (KT = I.kx): the forward one
+ * ending at s+KT-1 (vf) and the reverse one starting at s (vr), with the
+ * same results as gs_start on each.  An ACGT-only window takes one paired
+ * entry for both; a window with another base starts each candidate on its
+ * own (the 13-mer rule and the wildcard steps depend on where the base
+ * lies in each walk order). */
+template <int NSTOP>
+__device__ __forceinline__ void gs_start_pair(const GsDevIndex &I, const unsigned char *seq, int s,
+                                              int KT, int iL, bool vf, bool vr, GsStart &F,
+                                              GsStart &R, unsigned long long &w_kmer,
+                                              unsigned long long &w_blk)
+{
+    const int ef = s + KT - 1;
+    F.l = R.l = 1u;
+    F.u = R.u = 0u;
+    F.fcode = R.fcode = 4u;
+    F.ok = R.ok = F.alive = R.alive = false;
+    F.pos = ef - (GS_K0 - 1);
+    R.pos = s + (GS_K0 - 1);
+    if (!vf && !vr) return;
+    /* the reverse key: complement codes, R[s] at bits 0-1 */
+    uint32_t pr = 0;
+    bool bad = false;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        if (j < KT) {
+            const uint32_t c = gs_comp_code(seq[s + j]);
+            bad |= c > 3u;
+            pr |= (c & 3u) << (j << 1);
+        }
+    }
+    if (!bad) {
+        /* the forward key (R[s+KT-1] at bits 0-1) is pr's reverse complement */
+        const uint32_t pf = gs_kmer_rc(pr, KT);
+        const uint4 e = gs_ld_pair(&I.kmerx[pf]);
+        /* code 7 (interval too wide to pack): gs_start's own 13-mer start */
+        bool wide = false;
+        if (vf) {
+            F.ok = true;
+            wide = !gs_entry_start(e.x, e.y, ef, -1, KT, F);
+        }
+        if (vr) {
+            R.ok = true;
+            wide |= !gs_entry_start(e.z, e.w, s, 1, KT, R);
+        }
+        if (!wide) {
+            w_kmer++;
+            return;
+        }
+    }
+    /* (the work counters count one lookup per candidate here) */
+    if (vf) {
+        F = gs_start_apart<NSTOP>(I, seq, ef, true, KT, iL);
+        w_kmer++;
+    }
+    if (vr) {
+        R = gs_start_apart<NSTOP>(I, seq, s, false, KT, iL);
+        w_kmer++;
+    }
+}
+
 /* ------------------------------------------------------------------ */
 /* per-batch preparation: candidate slots and work items per read */
 
-__global__ void gs_prepare_kernel(const uint32_t *lengths, uint32_t n_reads, int k,
+__global__ void gs_prepare_kernel(const uint32_t *lengths, uint32_t n_reads, int k, int paired_kt,
                                   uint64_t *slot_n, uint32_t *item_n)
 {
     uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -252,14 +409,24 @@ __global__ void gs_prepare_kernel(const uint32_t *lengths, uint32_t n_reads, int
     uint32_t n = 0;
     if (r < n_reads && lengths[r] >= (uint32_t)k) n = lengths[r] - (uint32_t)k + 1u;
     slot_n[r] = 2ull * n;
-    item_n[r] = 2u * ((n + GS_CHUNK - 1) / GS_CHUNK);
+    if (paired_kt) {
+        /* windows s in [0, L-KT] (k >= KT, so L-KT+1 >= n) */
+        const uint32_t w = n ? lengths[r] - (uint32_t)paired_kt + 1u : 0u;
+        item_n[r] = (w + GS_PCHUNK - 1) / GS_PCHUNK;
+    } else {
+        item_n[r] = 2u * ((n + GS_CHUNK - 1) / GS_CHUNK);
+    }
 }
 
-int gs_launch_prepare(GsBatch &b, cudaStream_t st)
+int gs_launch_prepare(const GsDevIndex &I, GsBatch &b, int kernel, cudaStream_t st)
 {
     uint32_t n = b.n_reads + 1;
+    /* the batched start pass pairs each window's two candidates when it
+     * starts from the longer table */
+    b.paired = kernel == GS_KERNEL_BATCHED && I.kx > GS_K0 && gs_start_len_host(I, b.k) == I.kx;
     /* counts are written in place and scanned into offsets */
-    gs_prepare_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.lengths, b.n_reads, b.k, b.slot_off,
+    gs_prepare_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.lengths, b.n_reads, b.k,
+                                                        b.paired ? I.kx : 0, b.slot_off,
                                                         b.item_off);
     GS_CUDA(cudaGetLastError());
     return GS_OK;
@@ -337,7 +504,9 @@ __device__ __forceinline__ void gs_lockstep_item(const GsDevIndex &I, const GsBa
     const uint32_t chunk = fwd ? local : local - nch;
     const uint32_t ci = chunk * GS_CHUNK + (uint32_t)lane;
     const bool in_range = ci < n;
-    const bool owned = in_range && (lane < GS_CHUNK || ci == n - 1u);
+    /* lane 31 only starts the next item's first candidate (which that item
+     * owns: ceil(n / GS_CHUNK) items cover every candidate) */
+    const bool owned = in_range && lane < GS_CHUNK;
     const unsigned char *seq = (const unsigned char *)B.seqs + B.offsets[r];
     const int iL = (int)L;
 
@@ -832,7 +1001,9 @@ __device__ __forceinline__ void gs_start_item(const GsDevIndex &I, const GsBatch
     const uint32_t chunk = fwd ? local : local - nch;
     const uint32_t ci = chunk * GS_CHUNK + (uint32_t)lane;
     const bool in_range = ci < n;
-    const bool owned = in_range && (lane < GS_CHUNK || ci == n - 1u);
+    /* lane 31 only starts the next item's first candidate (which that item
+     * owns: ceil(n / GS_CHUNK) items cover every candidate) */
+    const bool owned = in_range && lane < GS_CHUNK;
     const unsigned char *seq = (const unsigned char *)B.seqs + B.offsets[r];
     const int iL = (int)L;
     const int anchor = fwd ? (k - 1 + (int)ci) : ((int)n - 1 - (int)ci);
@@ -917,7 +1088,126 @@ __device__ __forceinline__ void gs_start_item(const GsDevIndex &I, const GsBatch
     }
 }
 
+/* one walker-buffer entry of a warp's reservation (rank among the warp's
+ * walkers of this item), or the walk in place when the buffer is full */
 template <int NSTOP, int COUNT>
+__device__ __forceinline__ void gs_push_walker(const GsDevIndex &I, const GsBatch &B,
+                                               const GsReserve &res, uint32_t g, uint32_t rem,
+                                               uint32_t rank, uint32_t r, uint32_t n, bool fwd,
+                                               int anchor, int pos, uint32_t l, uint32_t u,
+                                               uint32_t jl, uint32_t ju, bool jpend, int iL,
+                                               unsigned long long &wb)
+{
+    uint64_t idx;
+    if (rank < rem) idx = res.next + rank;
+    else idx = (uint64_t)g + (rank - rem);
+    const uint64_t cap_end = rank < rem ? res.end : min((uint64_t)g + GS_WALKER_CHUNK, B.walker_cap);
+    /* the entry keeps 30 bits of anchor: reads of 2^30 bases or more (none
+     * in practice) are walked here */
+    if (idx < cap_end && iL < (1 << 30)) {
+        GsWalker w;
+        w.r = r;
+        w.anchor = (uint32_t)anchor | (fwd ? GS_WALKER_FWD : 0u) | (jpend ? GS_WALKER_JPEND : 0u);
+        w.l = l;
+        w.u = u;
+        w.jl = jl;
+        w.ju = ju;
+        B.walkers[idx] = w;
+    } else {
+        gs_walk_in_place<NSTOP, COUNT>(I, B, r, n, fwd, anchor, pos, l, u, jl, ju, jpend, wb);
+    }
+}
+
+/* J of an owned candidate from its neighbour's start, as in gs_start_item:
+ * a forced code settles containment, otherwise the neighbour's interval is
+ * J one base short (jpend) */
+__device__ __forceinline__ void gs_start_j(uint32_t cn, uint32_t fcode, bool nalive, uint32_t nl,
+                                           uint32_t nu, bool &killed, bool &jpend, uint32_t &jl,
+                                           uint32_t &ju)
+{
+    if (cn > 3u) return;
+    if (fcode < 4u) {
+        killed = (fcode == cn);
+    } else if (nalive) {
+        jl = nl;
+        ju = nu;
+        jpend = true;
+    }
+}
+
+/* A paired work item: the windows s = GS_PCHUNK*local - 1 + lane of read r
+ * (lanes 1..GS_PCHUNK own theirs; lanes 0 and 31 start their windows only
+ * for the neighbours' J), each window's forward candidate (ending at
+ * s+KT-1, neighbour e+1 = lane+1) and reverse candidate (starting at s,
+ * neighbour s-1 = lane-1) from one start-table entry.  Records, J and
+ * walkers are those of gs_start_item for each candidate. */
+template <int NSTOP, int COUNT>
+__device__ __forceinline__ void gs_start_pair_item(const GsDevIndex &I, const GsBatch &B, uint32_t r,
+                                                   uint32_t local, int lane, GsReserve &res,
+                                                   unsigned long long &wk, unsigned long long &wb)
+{
+    const int iL = (int)B.lengths[r];
+    const int k = B.k, KT = I.kx;
+    const uint32_t n = (uint32_t)(iL - k + 1);   /* candidates per strand (the item exists: L >= k) */
+    const int s = (int)(local * GS_PCHUNK) - 1 + lane;
+    const bool in_range = s >= 0 && s <= iL - KT;
+    const bool owned = in_range && lane >= 1 && lane <= GS_PCHUNK;
+    const bool vf = in_range && s >= k - KT;   /* forward candidate s+KT-1 >= k-1 */
+    const bool vr = in_range && s <= iL - k;   /* reverse candidate s <= L-k */
+    const unsigned char *seq = (const unsigned char *)B.seqs + B.offsets[r];
+    const int ef = s + KT - 1;
+    GsStart F, R;
+    gs_start_pair<NSTOP>(I, seq, s, KT, iL, vf, vr, F, R, wk, wb);
+    const uint32_t fnl = __shfl_down_sync(0xffffffffu, F.l, 1);
+    const uint32_t fnu = __shfl_down_sync(0xffffffffu, F.u, 1);
+    const int fna = __shfl_down_sync(0xffffffffu, F.alive ? 1 : 0, 1);
+    const uint32_t rnl = __shfl_up_sync(0xffffffffu, R.l, 1);
+    const uint32_t rnu = __shfl_up_sync(0xffffffffu, R.u, 1);
+    const int rna = __shfl_up_sync(0xffffffffu, R.alive ? 1 : 0, 1);
+
+    bool fk = false, fj = false, rk = false, rj = false;
+    uint32_t fjl = 1, fju = 0, rjl = 1, rju = 0;
+    if (owned && vf && F.alive && ef + 1 < iL)
+        gs_start_j(gs_fwd_code(seq[ef + 1]), F.fcode, fna != 0, fnl, fnu, fk, fj, fjl, fju);
+    if (owned && vr && R.alive && s >= 1)
+        gs_start_j(gs_comp_code(seq[s - 1]), R.fcode, rna != 0, rnl, rnu, rk, rj, rjl, rju);
+
+    const bool wf = owned && vf && F.alive && !fk;
+    const bool wr = owned && vr && R.alive && !rk;
+    if (owned && vf && !wf) gs_write_record(B, r, n, true, ef, F.pos, F.l, F.u, F.ok, fk);
+    if (owned && vr && !wr) gs_write_record(B, r, n, false, s, R.pos, R.l, R.u, R.ok, rk);
+    const uint32_t mf = __ballot_sync(0xffffffffu, wf), mr = __ballot_sync(0xffffffffu, wr);
+    if (!(mf | mr)) return;
+    const uint32_t lt = (1u << lane) - 1u;
+    const uint32_t cnt = (uint32_t)(__popc(mf) + __popc(mr));
+    const uint32_t rem = res.end - res.next;
+    uint32_t g = 0;
+    if (rem < cnt) {
+        if (res.full) {
+            g = (uint32_t)B.walker_cap;
+        } else {
+            if (lane == 0) g = atomicAdd(B.queue + 2, GS_WALKER_CHUNK);
+            g = __shfl_sync(0xffffffffu, g, 0);
+            if ((uint64_t)g + GS_WALKER_CHUNK >= B.walker_cap) res.full = 1u;
+        }
+    }
+    if (wf)
+        gs_push_walker<NSTOP, COUNT>(I, B, res, g, rem, (uint32_t)__popc(mf & lt), r, n, true, ef,
+                                     F.pos, F.l, F.u, fjl, fju, fj, iL, wb);
+    if (wr)
+        gs_push_walker<NSTOP, COUNT>(I, B, res, g, rem,
+                                     (uint32_t)(__popc(mf) + __popc(mr & lt)), r, n, false, s,
+                                     R.pos, R.l, R.u, rjl, rju, rj, iL, wb);
+    if (rem < cnt) {
+        res.next = (uint32_t)min((uint64_t)g + (cnt - rem), B.walker_cap);
+        res.end = (uint32_t)min((uint64_t)g + GS_WALKER_CHUNK, B.walker_cap);
+        if (res.next > res.end) res.next = res.end;
+    } else {
+        res.next += cnt;
+    }
+}
+
+template <int NSTOP, int COUNT, bool PAIRED>
 __global__ void __launch_bounds__(256, 3) gs_search_start(GsDevIndex I, GsBatch B, int queue_chunk)
 {
     const int lane = threadIdx.x & 31;
@@ -938,7 +1228,8 @@ __global__ void __launch_bounds__(256, 3) gs_search_start(GsDevIndex I, GsBatch 
         uint32_t r = lo;
         for (uint32_t it = first; it < last; it++) {
             while (B.item_off[r + 1] <= it) r++;
-            gs_start_item<NSTOP, COUNT>(I, B, r, it - B.item_off[r], lane, res, wk, wb);
+            if (PAIRED) gs_start_pair_item<NSTOP, COUNT>(I, B, r, it - B.item_off[r], lane, res, wk, wb);
+            else gs_start_item<NSTOP, COUNT>(I, B, r, it - B.item_off[r], lane, res, wk, wb);
         }
     }
     /* unused entries of the last reservation: holes */
@@ -1184,8 +1475,10 @@ static int gs_launch_batched(const GsDevIndex &I, GsBatch &B, int queue_chunk, i
     if (queue_chunk <= 0) queue_chunk = GS_QUEUE_CHUNK;
     const bool cnt = B.work != NULL, nstop = B.n_mode == GS_N_STOP;
     void (*start)(GsDevIndex, GsBatch, int) =
-        nstop ? (cnt ? gs_search_start<1, 1> : gs_search_start<1, 0>)
-              : (cnt ? gs_search_start<0, 1> : gs_search_start<0, 0>);
+        B.paired ? (nstop ? (cnt ? gs_search_start<1, 1, true> : gs_search_start<1, 0, true>)
+                          : (cnt ? gs_search_start<0, 1, true> : gs_search_start<0, 0, true>))
+                 : (nstop ? (cnt ? gs_search_start<1, 1, false> : gs_search_start<1, 0, false>)
+                          : (cnt ? gs_search_start<0, 1, false> : gs_search_start<0, 0, false>));
     void (*walk)(GsDevIndex, GsBatch) = nstop ? (cnt ? gs_search_walk<1, 1> : gs_search_walk<1, 0>)
                                               : (cnt ? gs_search_walk<0, 1> : gs_search_walk<0, 0>);
     if (ctas_per_sm <= 0) {
