@@ -758,8 +758,8 @@ def main():
                                       max(1, work["n_kmer"] + work["n_occ_blocks"])},
             "e2e": {"value": e2e_value, "unit": "reads/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            # prepare, start, walk, (text), finalize count + emit, expand, locate
-            "gpu_launches": (8 if text_on else 7) * args.steps,
+            # prepare, start, walk, (text), leftover, finalize count + emit, expand, locate
+            "gpu_launches": (9 if text_on else 8) * args.steps,
             "graph": "each timed step replays one CUDA graph of the whole pass",
             "clocks": clocks.summary(),
             "roofline": roofline,

@@ -749,7 +749,7 @@ static int enqueue_pass(gs_ctx *c, const char *d_seqs, const uint64_t *d_offsets
     GS_CUDA(cudaMemsetAsync(c->recmask, 0, ((c->cap_slots + 31) / 32 + 1) * sizeof(uint32_t), st));
     B.item_cap = c->g_items;
     /* the walker buffer as the sizing pass left it; walkers beyond it are
-     * walked in the start pass */
+     * left to the leftover pass */
     if (c->last_walker_cap && c->walkers) {
         B.walkers = c->walkers;
         B.walker_cap = c->last_walker_cap;

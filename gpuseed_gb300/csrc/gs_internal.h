@@ -121,7 +121,8 @@ struct GsBatch {
                                 * table entry for both strands' candidates (set by
                                 * gs_launch_prepare) */
     GsWalker *walkers;         /* batched search: survivors of the start pass */
-    uint64_t walker_cap;       /* entries allocated (0: every walk stays in the start pass) */
+    uint64_t walker_cap;       /* entries allocated (0: every walk is left to the leftover pass) */
+    uint32_t walker_chunk;     /* entries a start-pass warp reserves at a time */
     struct GsTextJob *text_jobs;   /* walkers handed to the text pass */
     uint64_t text_cap;         /* entries allocated (0: text mode stays inline) */
 };
@@ -134,6 +135,7 @@ struct GsTextJob {
 
 #define GS_FLAG_WALK 1u
 #define GS_FLAG_OVERFLOW 2u
+#define GS_FLAG_LEFTOVER 4u   /* the start pass left walks in record slots (leftover pass) */
 
 __host__ __device__ static inline uint32_t gs_fwd_code(unsigned char ch)
 {

@@ -713,15 +713,35 @@ __global__ void __launch_bounds__(256, 5) gs_search_lockstep(GsDevIndex I, GsBat
  *     otherwise the walker carries lane+1's start interval and its first
  *     step in the walk pass extends that to I's far end.  Survivors go to
  *     the walker buffer in per-warp reserved chunks (unused entries marked
- *     r = ~0); a walker that finds the buffer full is walked in place.
+ *     r = ~0); a walker that finds the buffer full is left in its record
+ *     slot for gs_search_leftover, which walks it without J.
  *   gs_search_walk: one walker per lane, each lane refilled as soon as its
  *     walker ends, from a per-warp window of the buffer. */
 
 #define GS_WALKER_HOLE 0xffffffffu
 #define GS_WALKER_JPEND 0x40000000u   /* anchor flag: J is one base short of I's far end */
 #define GS_WALKER_FWD 0x80000000u
-#define GS_WALKER_CHUNK 512u      /* buffer entries a warp reserves at a time */
-#define GS_WALK_WINDOW 512u       /* buffer entries a walk-pass warp takes at a time */
+#define GS_WALKER_CHUNK 512u      /* most buffer entries a warp reserves at a time */
+
+/* entries a start-pass warp reserves at a time (gs_launch_batched sets it) */
+__device__ __forceinline__ uint32_t gs_walker_chunk(const GsBatch &B)
+{
+    return B.walker_chunk;
+}
+
+/* Sizes from the walker buffer's capacity and a grid of `warps` warps,
+ * multiples of 32 from 32 to `most`: about 1/`parts` of a warp's share, so
+ * that a small batch's buffer (start reservations) or walkers (walk-pass
+ * windows) spread over every warp */
+static uint32_t gs_share_size(uint64_t cap, uint32_t warps, uint32_t parts, uint32_t most)
+{
+    uint64_t v = cap / ((uint64_t)warps * parts);
+    v &= ~31ull;
+    if (v < 32u) v = 32u;
+    if (v > most) v = most;
+    return (uint32_t)v;
+}
+#define GS_WALK_WINDOW 512u       /* most buffer entries a walk-pass warp takes at a time */
 
 /* Text mode.  A walker whose interval is one row [l,l] and whose J is
  * empty can no longer be contained: its walk only extends one occurrence,
@@ -962,23 +982,29 @@ __device__ __forceinline__ bool gs_walk_step(const GsDevIndex &I, const unsigned
     return true;
 }
 
-/* a walk that did not fit the walker buffer, finished by the start pass
- * (kept out of line: it is the rare path and would cost the start pass
- * registers) */
-template <int NSTOP, int COUNT>
-__device__ __noinline__ void gs_walk_in_place(const GsDevIndex &I, const GsBatch &B, uint32_t r,
-                                               uint32_t n, bool fwd, int anchor, int pos,
-                                               uint32_t l, uint32_t u, uint32_t jl, uint32_t ju,
-                                               bool jpend, unsigned long long &wb)
+/* A walk that found no room in the walker buffer: its start interval goes
+ * to its own record slot under GS_LEFTOVER_MARK (no record has x = y = ~0),
+ * and gs_search_leftover walks it after the other passes (its start and J
+ * made again from the read). */
+#define GS_LEFTOVER_MARK 0xffffffffu
+
+__device__ __forceinline__ void gs_write_leftover(const GsBatch &B, uint32_t r, uint32_t n, bool fwd,
+                                                  int anchor, uint32_t l, uint32_t u)
 {
-    const unsigned char *seq = (const unsigned char *)B.seqs + B.offsets[r];
-    const int iL = (int)B.lengths[r];
-    const int dir = fwd ? -1 : 1;
-    bool killed = false;
-    while (gs_walk_step<NSTOP, COUNT, true>(I, seq, iL, fwd, dir, l, u, jl, ju, pos, jpend, killed,
-                                            wb)) {
+    const uint64_t slot = B.slot_off[r] + (fwd ? (uint64_t)(anchor - (B.k - 1))
+                                               : (uint64_t)n + (uint64_t)anchor);
+    if (slot < B.slot_cap) {
+        GsRec rec;
+        rec.x = (int32_t)GS_LEFTOVER_MARK;
+        rec.y = (int32_t)GS_LEFTOVER_MARK;
+        rec.l = l;
+        rec.u = u;
+        B.slots[slot] = rec;
+        atomicOr(B.recmask + (slot >> 5), 1u << (slot & 31u));
+        atomicOr(B.queue + 1, GS_FLAG_LEFTOVER);
+    } else {
+        atomicOr(B.queue + 1, GS_FLAG_OVERFLOW);
     }
-    gs_write_record(B, r, n, fwd, anchor, pos, l, u, true, killed);
 }
 
 /* per-warp reservation of walker-buffer entries: [next, end); full once a
@@ -1054,18 +1080,18 @@ __device__ __forceinline__ void gs_start_item(const GsDevIndex &I, const GsBatch
         if (res.full) {
             g = (uint32_t)B.walker_cap;
         } else {
-            if (lane == 0) g = atomicAdd(B.queue + 2, GS_WALKER_CHUNK);
+            if (lane == 0) g = atomicAdd(B.queue + 2, gs_walker_chunk(B));
             g = __shfl_sync(0xffffffffu, g, 0);
-            if ((uint64_t)g + GS_WALKER_CHUNK >= B.walker_cap) res.full = 1u;
+            if ((uint64_t)g + gs_walker_chunk(B) >= B.walker_cap) res.full = 1u;
         }
     }
     if (walker) {
         uint64_t idx;
         if (rank < rem) idx = res.next + rank;
         else idx = (uint64_t)g + (rank - rem);
-        const uint64_t cap_end = rank < rem ? res.end : min((uint64_t)g + GS_WALKER_CHUNK, B.walker_cap);
+        const uint64_t cap_end = rank < rem ? res.end : min((uint64_t)g + gs_walker_chunk(B), B.walker_cap);
         /* the entry keeps 30 bits of anchor: reads of 2^30 bases or more
-         * (none in practice) are walked here */
+         * (none in practice) are left over too */
         if (idx < cap_end && iL < (1 << 30)) {
             GsWalker w;
             w.r = r;
@@ -1076,12 +1102,12 @@ __device__ __forceinline__ void gs_start_item(const GsDevIndex &I, const GsBatch
             w.ju = ju;
             B.walkers[idx] = w;
         } else {
-            gs_walk_in_place<NSTOP, COUNT>(I, B, r, n, fwd, anchor, pos, l, u, jl, ju, jpend, wb);
+            gs_write_leftover(B, r, n, fwd, anchor, l, u);
         }
     }
     if (rem < cnt) {
         res.next = (uint32_t)min((uint64_t)g + (cnt - rem), B.walker_cap);
-        res.end = (uint32_t)min((uint64_t)g + GS_WALKER_CHUNK, B.walker_cap);
+        res.end = (uint32_t)min((uint64_t)g + gs_walker_chunk(B), B.walker_cap);
         if (res.next > res.end) res.next = res.end;
     } else {
         res.next += cnt;
@@ -1089,33 +1115,27 @@ __device__ __forceinline__ void gs_start_item(const GsDevIndex &I, const GsBatch
 }
 
 /* one walker-buffer entry of a warp's reservation (rank among the warp's
- * walkers of this item), or the walk in place when the buffer is full */
-template <int NSTOP, int COUNT>
-__device__ __forceinline__ void gs_push_walker(const GsDevIndex &I, const GsBatch &B,
-                                               const GsReserve &res, uint32_t g, uint32_t rem,
-                                               uint32_t rank, uint32_t r, uint32_t n, bool fwd,
-                                               int anchor, int pos, uint32_t l, uint32_t u,
-                                               uint32_t jl, uint32_t ju, bool jpend, int iL,
-                                               unsigned long long &wb)
+ * walkers of this item); false when the buffer is full (or the read too
+ * long for the entry's anchor bits): the walk is then left over */
+__device__ __forceinline__ bool gs_push_walker(const GsBatch &B, const GsReserve &res, uint32_t g,
+                                               uint32_t rem, uint32_t rank, uint32_t r, bool fwd,
+                                               int anchor, uint32_t l, uint32_t u, uint32_t jl,
+                                               uint32_t ju, bool jpend, int iL)
 {
     uint64_t idx;
     if (rank < rem) idx = res.next + rank;
     else idx = (uint64_t)g + (rank - rem);
-    const uint64_t cap_end = rank < rem ? res.end : min((uint64_t)g + GS_WALKER_CHUNK, B.walker_cap);
-    /* the entry keeps 30 bits of anchor: reads of 2^30 bases or more (none
-     * in practice) are walked here */
-    if (idx < cap_end && iL < (1 << 30)) {
-        GsWalker w;
-        w.r = r;
-        w.anchor = (uint32_t)anchor | (fwd ? GS_WALKER_FWD : 0u) | (jpend ? GS_WALKER_JPEND : 0u);
-        w.l = l;
-        w.u = u;
-        w.jl = jl;
-        w.ju = ju;
-        B.walkers[idx] = w;
-    } else {
-        gs_walk_in_place<NSTOP, COUNT>(I, B, r, n, fwd, anchor, pos, l, u, jl, ju, jpend, wb);
-    }
+    const uint64_t cap_end = rank < rem ? res.end : min((uint64_t)g + gs_walker_chunk(B), B.walker_cap);
+    if (idx >= cap_end || iL >= (1 << 30)) return false;
+    GsWalker w;
+    w.r = r;
+    w.anchor = (uint32_t)anchor | (fwd ? GS_WALKER_FWD : 0u) | (jpend ? GS_WALKER_JPEND : 0u);
+    w.l = l;
+    w.u = u;
+    w.jl = jl;
+    w.ju = ju;
+    B.walkers[idx] = w;
+    return true;
 }
 
 /* J of an owned candidate from its neighbour's start, as in gs_start_item:
@@ -1186,21 +1206,20 @@ __device__ __forceinline__ void gs_start_pair_item(const GsDevIndex &I, const Gs
         if (res.full) {
             g = (uint32_t)B.walker_cap;
         } else {
-            if (lane == 0) g = atomicAdd(B.queue + 2, GS_WALKER_CHUNK);
+            if (lane == 0) g = atomicAdd(B.queue + 2, gs_walker_chunk(B));
             g = __shfl_sync(0xffffffffu, g, 0);
-            if ((uint64_t)g + GS_WALKER_CHUNK >= B.walker_cap) res.full = 1u;
+            if ((uint64_t)g + gs_walker_chunk(B) >= B.walker_cap) res.full = 1u;
         }
     }
-    if (wf)
-        gs_push_walker<NSTOP, COUNT>(I, B, res, g, rem, (uint32_t)__popc(mf & lt), r, n, true, ef,
-                                     F.pos, F.l, F.u, fjl, fju, fj, iL, wb);
-    if (wr)
-        gs_push_walker<NSTOP, COUNT>(I, B, res, g, rem,
-                                     (uint32_t)(__popc(mf) + __popc(mr & lt)), r, n, false, s,
-                                     R.pos, R.l, R.u, rjl, rju, rj, iL, wb);
+    if (wf && !gs_push_walker(B, res, g, rem, (uint32_t)__popc(mf & lt), r, true, ef, F.l, F.u,
+                              fjl, fju, fj, iL))
+        gs_write_leftover(B, r, n, true, ef, F.l, F.u);
+    if (wr && !gs_push_walker(B, res, g, rem, (uint32_t)(__popc(mf) + __popc(mr & lt)), r, false,
+                              s, R.l, R.u, rjl, rju, rj, iL))
+        gs_write_leftover(B, r, n, false, s, R.l, R.u);
     if (rem < cnt) {
         res.next = (uint32_t)min((uint64_t)g + (cnt - rem), B.walker_cap);
-        res.end = (uint32_t)min((uint64_t)g + GS_WALKER_CHUNK, B.walker_cap);
+        res.end = (uint32_t)min((uint64_t)g + gs_walker_chunk(B), B.walker_cap);
         if (res.next > res.end) res.next = res.end;
     } else {
         res.next += cnt;
@@ -1238,7 +1257,7 @@ __global__ void __launch_bounds__(256, 3) gs_search_start(GsDevIndex I, GsBatch 
 }
 
 template <int NSTOP, int COUNT>
-__global__ void __launch_bounds__(128, 8) gs_search_walk(GsDevIndex I, GsBatch B)
+__global__ void __launch_bounds__(128, 8) gs_search_walk(GsDevIndex I, GsBatch B, uint32_t wsz)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
@@ -1259,14 +1278,14 @@ __global__ void __launch_bounds__(128, 8) gs_search_walk(GsDevIndex I, GsBatch B
         while (need && !exhausted) {
             if (win == win_end) {
                 uint32_t g = 0;
-                if (lane == 0) g = atomicAdd(B.queue + 3, GS_WALK_WINDOW);
+                if (lane == 0) g = atomicAdd(B.queue + 3, wsz);
                 g = __shfl_sync(0xffffffffu, g, 0);
                 if (g >= n_w) {
                     exhausted = true;
                     break;
                 }
                 win = g;
-                win_end = min(g + GS_WALK_WINDOW, n_w);
+                win_end = min(g + wsz, n_w);
             }
             const uint32_t take = min((uint32_t)__popc(need), win_end - win);
             const uint32_t rank = __popc(need & lt);
@@ -1378,6 +1397,66 @@ __global__ void __launch_bounds__(256) gs_search_text(GsDevIndex I, GsBatch B)
 /* ------------------------------------------------------------------ */
 /* plain search: one read per thread */
 
+/* Leftover pass: the walks the start pass left in their record slots
+ * (GS_LEFTOVER_MARK), a warp per read, each slot's walk on one lane, started
+ * again with its J as the start pass would have made it; the slot gets the
+ * walk's record, or loses its record bit.  Returns at once when the start
+ * pass left none. */
+template <int NSTOP, int COUNT>
+__global__ void __launch_bounds__(256) gs_search_leftover(GsDevIndex I, GsBatch B)
+{
+    if (!(*(volatile uint32_t *)(B.queue + 1) & GS_FLAG_LEFTOVER)) return;
+    const int lane = threadIdx.x & 31;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int k = B.k, KT = gs_start_len(I, k);
+    unsigned long long wk = 0, wb = 0;
+    for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < B.n_reads; r += nwarps) {
+        const uint64_t base = B.slot_off[r], end = B.slot_off[r + 1];
+        if (end > B.slot_cap) continue;
+        const uint32_t n = (uint32_t)((end - base) >> 1);
+        const int iL = (int)B.lengths[r];
+        const unsigned char *seq = (const unsigned char *)B.seqs + B.offsets[r];
+        for (uint32_t j = (uint32_t)lane; j < 2u * n; j += 32) {
+            const uint64_t slot = base + j;
+            if (!((B.recmask[slot >> 5] >> (slot & 31u)) & 1u)) continue;
+            const GsRec rec = B.slots[slot];
+            if ((uint32_t)rec.x != GS_LEFTOVER_MARK || (uint32_t)rec.y != GS_LEFTOVER_MARK) continue;
+            const bool fwd = j < n;
+            /* slot j: forward e = k-1+j, reverse s = j-n (gs_write_record) */
+            const int anchor = fwd ? k - 1 + (int)j : (int)(j - n);
+            const int dir = fwd ? -1 : 1;
+            /* the walker as the start pass made it: its start, and J from
+             * the start of its neighbour toward the longer match (gs_start_item) */
+            uint32_t l, u, fcode, jl = 1u, ju = 0u;
+            int pos;
+            bool alive, contained, jpend = false, killed = false;
+            gs_start<NSTOP, false>(I, seq, anchor, dir, fwd, KT, iL, l, u, pos, alive, contained,
+                                   fcode, wk, wb);
+            const int nb = anchor - dir;
+            if (alive && fcode >= 4u && nb >= 0 && nb < iL &&
+                (fwd ? gs_fwd_code(seq[nb]) : gs_comp_code(seq[nb])) <= 3u) {
+                uint32_t nl, nu, nfc;
+                int npos;
+                bool nalive, ncont;
+                gs_start<NSTOP, false>(I, seq, nb, dir, fwd, KT, iL, nl, nu, npos, nalive, ncont,
+                                       nfc, wk, wb);
+                if (nalive) {
+                    jl = nl;
+                    ju = nu;
+                    jpend = true;
+                }
+            }
+            while (alive && gs_walk_step<NSTOP, COUNT, true>(I, seq, iL, fwd, dir, l, u, jl, ju, pos,
+                                                             jpend, killed, wb)) {
+            }
+            /* no record: drop the slot's bit (gs_write_record leaves it) */
+            atomicAnd(B.recmask + (slot >> 5), ~(1u << (slot & 31u)));
+            gs_write_record(B, r, n, fwd, anchor, pos, l, u, true, killed);
+        }
+    }
+    if (COUNT) gs_add_work(B, wk, wb);
+}
+
 template <int NSTOP>
 __global__ void __launch_bounds__(128) gs_search_plain(GsDevIndex I, GsBatch B)
 {
@@ -1479,8 +1558,9 @@ static int gs_launch_batched(const GsDevIndex &I, GsBatch &B, int queue_chunk, i
                           : (cnt ? gs_search_start<0, 1, true> : gs_search_start<0, 0, true>))
                  : (nstop ? (cnt ? gs_search_start<1, 1, false> : gs_search_start<1, 0, false>)
                           : (cnt ? gs_search_start<0, 1, false> : gs_search_start<0, 0, false>));
-    void (*walk)(GsDevIndex, GsBatch) = nstop ? (cnt ? gs_search_walk<1, 1> : gs_search_walk<1, 0>)
-                                              : (cnt ? gs_search_walk<0, 1> : gs_search_walk<0, 0>);
+    void (*walk)(GsDevIndex, GsBatch, uint32_t) =
+        nstop ? (cnt ? gs_search_walk<1, 1> : gs_search_walk<1, 0>)
+              : (cnt ? gs_search_walk<0, 1> : gs_search_walk<0, 0>);
     if (ctas_per_sm <= 0) {
         int occ = 0;
         GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, start, 256, 0));
@@ -1494,12 +1574,16 @@ static int gs_launch_batched(const GsDevIndex &I, GsBatch &B, int queue_chunk, i
     if (grid == 0) grid = 1;
     GS_CUDA(cudaMemsetAsync(B.queue, 0, sizeof(uint32_t), st));
     GS_CUDA(cudaMemsetAsync(B.queue + 2, 0, 2 * sizeof(uint32_t), st));
+    B.walker_chunk = gs_share_size(B.walker_cap, grid * 8u, 16u, GS_WALKER_CHUNK);
     start<<<grid, 256, 0, st>>>(I, B, queue_chunk);
     GS_CUDA(cudaGetLastError());
     if (B.walker_cap) {
         int wocc = 0;
         GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&wocc, walk, 128, 0));
-        walk<<<(uint32_t)sms * (uint32_t)(wocc > 0 ? wocc : 4), 128, 0, st>>>(I, B);
+        const uint32_t wgrid = (uint32_t)sms * (uint32_t)(wocc > 0 ? wocc : 4);
+        /* the buffer's capacity stands for its walkers (the count is on the
+         * device): about an eighth of a warp's share a window */
+        walk<<<wgrid, 128, 0, st>>>(I, B, gs_share_size(B.walker_cap, wgrid * 4u, 8u, GS_WALK_WINDOW));
         GS_CUDA(cudaGetLastError());
         if (B.text_cap) {
             void (*text)(GsDevIndex, GsBatch) =
@@ -1509,6 +1593,11 @@ static int gs_launch_batched(const GsDevIndex &I, GsBatch &B, int queue_chunk, i
             GS_CUDA(cudaGetLastError());
         }
     }
+    void (*leftover)(GsDevIndex, GsBatch) =
+        nstop ? (cnt ? gs_search_leftover<1, 1> : gs_search_leftover<1, 0>)
+              : (cnt ? gs_search_leftover<0, 1> : gs_search_leftover<0, 0>);
+    leftover<<<(uint32_t)sms * 8u, 256, 0, st>>>(I, B);
+    GS_CUDA(cudaGetLastError());
     return GS_OK;
 }
 

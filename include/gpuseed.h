@@ -88,8 +88,8 @@ typedef struct {
                                fall back to a sized pass and a new capture */
     int32_t walker_slots;   /* batched: walker buffer entries per 16 work items of 31
                                candidates, a work item of 30 read windows (both strands)
-                               counting as two (0 = auto, 256; <0 = none: every walk stays
-                               in the start pass) */
+                               counting as two (0 = auto, 256; <0 = none: walks that
+                               outlast their start run in a later pass, unpruned) */
     int32_t max_occ;        /* > 0: drop output seeds whose interval has more rows than this
                                (bwa's -c; applied after the filters, the other seeds are
                                unchanged); 0 = off, the reference's output */

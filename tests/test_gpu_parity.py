@@ -325,7 +325,8 @@ def test_longer_start_table(small, kx):
                         ob = small["oidx"].seed(seqs, offs, lens, k=k, smem=smem, n_mode=n_mode)
                         assert_same(gres, ob, len(reads), f"kx={kx} kernel={kernel} k={k} n={n_mode}")
         # k > kx: the batched start pairs each window's two candidates; with
-        # a walker buffer of a few entries, or none, they walk in place
+        # a walker buffer of a few entries, or none, they are left to the
+        # leftover pass, which walks them without J
         for slots in (1, -1):
             for n_mode in (0, 1):
                 gres = small["ctx"].seed(seqs, offs, lens, k=kx + 3, smem=True, n_mode=n_mode,
