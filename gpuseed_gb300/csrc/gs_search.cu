@@ -13,10 +13,11 @@
  * The reference prunes with 30 warp shuffles per step over uninitialised
  * flags (:2100-2204); this file uses a defined rule with three launch forms:
  *
- *   GS_KERNEL_BATCHED (default): gs_search_start + gs_search_walk.  Each
- *     candidate carries the interval of its neighbour's string at its own
- *     far end and stops exactly where the rule says; candidates are started
- *     a warp per work item and walked one per lane (see "batched search").
+ *   GS_KERNEL_BATCHED (default): gs_search_start + gs_search_walk (+
+ *     gs_search_text, gs_search_leftover).  Each candidate carries the
+ *     interval of its neighbour's string at its own far end and stops
+ *     exactly where the rule says; candidates are started a warp per work
+ *     item and walked one per lane (see "batched search").
  *   GS_KERNEL_LOCKSTEP: gs_search_lockstep + gs_search_tail.  Persistent
  *     CTAs; each warp takes work items (read, strand, 31 candidates + 1
  *     helper lane) from a global queue and steps its 32 candidates in
@@ -706,17 +707,21 @@ __global__ void __launch_bounds__(256, 5) gs_search_lockstep(GsDevIndex I, GsBat
  * seeing its neighbour: no lockstep, no helper lane walking, no history.
  * J's bounds share occurrence blocks with I's whenever I is narrow.
  *
- *   gs_search_start: a warp per work item (31 candidates + the next item's
- *     first, started for its interval only), one round of start-table
- *     lookups.  The forced-extension code settles J where it can (forced to
- *     the neighbour's base: contained, stop; forced elsewhere: no J);
- *     otherwise the walker carries lane+1's start interval and its first
- *     step in the walk pass extends that to I's far end.  Survivors go to
- *     the walker buffer in per-warp reserved chunks (unused entries marked
- *     r = ~0); a walker that finds the buffer full is left in its record
- *     slot for gs_search_leftover, which walks it without J.
+ *   gs_search_start: a warp per work item, one round of start-table
+ *     lookups.  With the longer start table (k > kx) an item is 30 read
+ *     windows (+ a helper window on each side) and one paired entry starts
+ *     a window's forward and reverse candidate (gs_start_pair_item); else
+ *     31 candidates of one strand + the next item's first, started for its
+ *     interval only (gs_start_item).  The forced-extension code settles J
+ *     where it can (forced to the neighbour's base: contained, stop; forced
+ *     elsewhere: no J); otherwise the walker carries its neighbour's start
+ *     interval and its first step in the walk pass extends that to I's far
+ *     end.  Survivors go to the walker buffer in per-warp reserved chunks
+ *     (unused entries marked r = ~0); a walker that finds the buffer full is
+ *     left in its record slot for gs_search_leftover.
  *   gs_search_walk: one walker per lane, each lane refilled as soon as its
- *     walker ends, from a per-warp window of the buffer. */
+ *     walker ends, from a per-warp window of the buffer; walkers that reach
+ *     one row without J go to gs_search_text. */
 
 #define GS_WALKER_HOLE 0xffffffffu
 #define GS_WALKER_JPEND 0x40000000u   /* anchor flag: J is one base short of I's far end */

@@ -156,12 +156,14 @@ int gs_index_kmer_table(const gs_index *idx, uint64_t first, uint64_t count, uin
 int gs_index_build(const uint8_t *codes, uint64_t n, uint32_t sa_intv, int device,
                    const char *prefix, gs_index **out);
 /* Length of the k-mer start table (13..16).  Loading picks 16 above 2^30
- * bases, 15 above 2^28, 14 above 2^26, else 13 (8 * 4^len bytes of HBM; a
- * lower length is taken when the memory is not there).  A candidate starts
- * from the interval of its first len bases instead of 13 + len-13 steps: the
- * SA interval of a string does not depend on how it is found, so results do
- * not change; seeding uses it only when k > len.  Call while no pass runs on
- * a context of this index. */
+ * bases, 15 above 2^28, 14 above 2^26, else 13 (16 * 4^len bytes of HBM:
+ * each len-mer's entry and its reverse complement's, so that one lookup
+ * starts both strands' candidates of a read window; a lower length is taken
+ * when the memory is not there).  A candidate starts from the interval of
+ * its first len bases instead of 13 + len-13 steps: the SA interval of a
+ * string does not depend on how it is found, so results do not change;
+ * seeding uses it only when k > len.  Call while no pass runs on a context
+ * of this index. */
 int gs_index_set_kmer_len(gs_index *idx, int kmer_len);
 /* Text structures in HBM, built from the .bwt and .sa by one pass of LF
  * chains: 4 * seq_len bytes of full suffix array, seq_len / 4 of packed
