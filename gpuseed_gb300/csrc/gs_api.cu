@@ -16,7 +16,9 @@
  */
 #include "gs_internal.h"
 
-#define GS_SEED_CHUNK_READS (1u << 21)   /* gs_seed runs batches of twice this in chunks */
+#define GS_SEED_CHUNK_READS (1u << 22)   /* gs_seed runs batches of this or more in chunks:
+                                            the middle ones of about this many reads */
+#define GS_SEED_END_FRACTION 0.1         /* the first and the last chunk, of a middle one */
 #define GS_SEED_MAX_CHUNKS 16
 
 #include <cub/cub.cuh>
@@ -878,14 +880,16 @@ extern "C" int gs_seed_device(gs_ctx *c, const char *d_seqs, const uint64_t *d_o
 static int seed_chunked(gs_ctx *c, const char *seqs, const uint64_t *offsets, uint32_t n_reads,
                         const gs_params *p, uint64_t bytes)
 {
-    /* the first and the last chunk are half-size: the first one's copy-in
-     * and the last one's copy-out are the only copies nothing overlaps */
+    /* the first and the last chunk are small: the first one's copy-in and
+     * the last one's copy-out are the only copies nothing overlaps, and
+     * every chunk costs its pass's fixed part (host syncs, kernel tails) */
     uint32_t K = (n_reads + GS_SEED_CHUNK_READS - 1) / GS_SEED_CHUNK_READS + 1;
     if (K > GS_SEED_MAX_CHUNKS) K = GS_SEED_MAX_CHUNKS;
     uint32_t first[GS_SEED_MAX_CHUNKS + 1];
+    const double m = (double)n_reads / ((double)K - 2.0 + 2.0 * GS_SEED_END_FRACTION);
     first[0] = 0;
     for (uint32_t j = 1; j < K; j++)
-        first[j] = (uint32_t)((uint64_t)n_reads * (2 * j - 1) / (2 * (K - 1)));
+        first[j] = (uint32_t)(GS_SEED_END_FRACTION * m + (double)(j - 1) * m);
     first[K] = n_reads;
     uint32_t max_n = 0;
     for (uint32_t j = 0; j < K; j++)
@@ -985,7 +989,7 @@ extern "C" int gs_seed(gs_ctx *c, const char *seqs, const uint64_t *offsets,
         bytes = c->h_small[12];
         /* chunks would cut the reference's cross-read neighbour scan */
         const bool cross = !p->smem && p->mem_next == GS_MEM_NEXT_GPUSEED;
-        if (n_reads >= 2 * GS_SEED_CHUNK_READS && c->h_small[13] == 0 && !cross)
+        if (n_reads >= GS_SEED_CHUNK_READS && c->h_small[13] == 0 && !cross)
             return seed_chunked(c, seqs, offsets, n_reads, p, bytes);
     }
     RC(grow(c->d_seqs, c->cap_seqs, bytes + 1, c->st));
