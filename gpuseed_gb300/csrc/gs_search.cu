@@ -292,12 +292,7 @@ __device__ __forceinline__ bool gs_start(const GsDevIndex &I, const unsigned cha
 }
 
 /* start-table length used for minimum seed length k */
-__device__ __forceinline__ int gs_start_len(const GsDevIndex &I, int k)
-{
-    return (I.kx > GS_K0 && k > I.kx) ? I.kx : GS_K0;
-}
-
-static inline int gs_start_len_host(const GsDevIndex &I, int k)
+__host__ __device__ __forceinline__ int gs_start_len(const GsDevIndex &I, int k)
 {
     return (I.kx > GS_K0 && k > I.kx) ? I.kx : GS_K0;
 }
@@ -424,7 +419,7 @@ int gs_launch_prepare(const GsDevIndex &I, GsBatch &b, int kernel, cudaStream_t 
     uint32_t n = b.n_reads + 1;
     /* the batched start pass pairs each window's two candidates when it
      * starts from the longer table */
-    b.paired = kernel == GS_KERNEL_BATCHED && I.kx > GS_K0 && gs_start_len_host(I, b.k) == I.kx;
+    b.paired = kernel == GS_KERNEL_BATCHED && I.kx > GS_K0 && gs_start_len(I, b.k) == I.kx;
     /* counts are written in place and scanned into offsets */
     gs_prepare_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.lengths, b.n_reads, b.k,
                                                         b.paired ? I.kx : 0, b.slot_off,
