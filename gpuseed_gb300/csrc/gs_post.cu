@@ -6,9 +6,9 @@
  * segmented sorts by begin (:1233, :3570) and the expansion + locate kernels
  * (:555-724):
  *
- *   gs_finalize_count  warp per read: compacts the read's candidate slots in
- *                      place (ballot prefix) and counts the seeds/positions
- *                      the filters keep;
+ *   gs_finalize_count  lane per read (warp per long read): compacts the
+ *                      read's candidate slots in place and counts the
+ *                      seeds/positions the filters keep;
  *   (scan)             exclusive sums of those counts over reads;
  *   gs_finalize_emit   thread per read: merges the forward (ascending end)
  *                      and reverse (ascending start) records by begin --
@@ -223,92 +223,171 @@ __device__ __forceinline__ void gs_warp_compact_both(GsRec *slots, const uint32_
     }
 }
 
+/* One strand of a read -- slots s0..s0+n -- compacted in place by one
+ * thread: each flagged record moves to s0 + (its rank), in order, and the
+ * rule decides it once its neighbour is known (forward: the next record,
+ * one record behind; reverse: the previous one).  Adds the kept seeds and
+ * their positions; returns the record count. */
+__device__ __forceinline__ uint32_t gs_lane_compact(GsRec *slots, const uint32_t *mask, uint64_t s0,
+                                                    uint32_t n, bool fwd, int smem,
+                                                    uint32_t max_occ, uint64_t &seeds,
+                                                    uint64_t &npos)
+{
+    const uint64_t s1 = s0 + n;
+    uint32_t cnt = 0;
+    GsRec prev;
+    prev.x = prev.y = 0;
+    prev.l = 1u;
+    prev.u = 0u;
+    bool keep;
+    uint32_t c, xl, xu;
+    for (uint64_t lo = s0 & ~31ull; lo < s1; lo += 32) {
+        uint32_t m = mask[lo >> 5];
+        if (lo < s0) m &= 0xffffffffu << (uint32_t)(s0 - lo);
+        if (lo + 32 > s1) m &= 0xffffffffu >> (uint32_t)(lo + 32 - s1);
+        while (m) {
+            const uint32_t b = (uint32_t)__ffs(m) - 1u;
+            m &= m - 1u;
+            const GsRec rec = slots[lo + b];
+            slots[s0 + cnt] = rec;   /* at or before its source: read already */
+            if (fwd) {
+                if (cnt) gs_fwd_rule_v(prev, rec, true, smem, max_occ, keep, c, xl, xu);
+            } else {
+                gs_rev_rule_v(rec, prev, cnt > 0, smem, max_occ, keep, c, xl, xu);
+            }
+            if ((!fwd || cnt) && keep && c) {
+                seeds++;
+                npos += c;
+            }
+            prev = rec;
+            cnt++;
+        }
+    }
+    if (fwd && cnt) {
+        gs_fwd_rule_v(prev, prev, false, smem, max_occ, keep, c, xl, xu);
+        if (keep && c) {
+            seeds++;
+            npos += c;
+        }
+    }
+    return cnt;
+}
+
+/* reads whose two strands span at most this many slots are compacted by one
+ * lane; longer ones by the whole warp */
+#define GS_LANE_SLOTS 512u
+
+/* a read compacted and counted by the whole warp (long reads) */
+__device__ __noinline__ void gs_finalize_read_warp(const GsBatch &B, uint32_t r, uint64_t base,
+                                                   uint64_t next, int lane)
+{
+    uint32_t n = (uint32_t)((next - base) >> 1);
+    GsRec *F = B.slots + base;
+    GsRec *Rv = F + n;
+    uint32_t nf, nr;
+    uint64_t seeds = 0, npos = 0;
+    bool done = false;
+    if (2u * n + 31u <= 1024u) {
+        GsRec mine;
+        gs_warp_compact_both(B.slots, B.recmask, base, n, lane, nf, nr, mine);
+        if (nf + nr <= 32u) {
+            /* lane j holds record j of [forward | reverse]: the rules'
+             * neighbours are lanes j+1 (forward) and j-1 (reverse) */
+            GsRec up, dn;
+            up.x = __shfl_down_sync(0xffffffffu, mine.x, 1);
+            up.y = __shfl_down_sync(0xffffffffu, mine.y, 1);
+            up.l = __shfl_down_sync(0xffffffffu, mine.l, 1);
+            up.u = __shfl_down_sync(0xffffffffu, mine.u, 1);
+            dn.x = __shfl_up_sync(0xffffffffu, mine.x, 1);
+            dn.y = __shfl_up_sync(0xffffffffu, mine.y, 1);
+            dn.l = __shfl_up_sync(0xffffffffu, mine.l, 1);
+            dn.u = __shfl_up_sync(0xffffffffu, mine.u, 1);
+            const uint32_t j = (uint32_t)lane;
+            bool keep = false;
+            uint32_t cnt = 0, xl, xu;
+            if (j < nf)
+                gs_fwd_rule_v(mine, up, j + 1 < nf, B.smem, B.max_occ, keep, cnt, xl, xu);
+            else if (j < nf + nr)
+                gs_rev_rule_v(mine, dn, j > nf, B.smem, B.max_occ, keep, cnt, xl, xu);
+            if (keep && cnt) {
+                seeds = 1;
+                npos = cnt;
+            }
+            done = true;
+        }
+    } else {
+        nf = gs_warp_compact(B.slots, B.recmask, base, n, lane);
+        nr = gs_warp_compact(B.slots, B.recmask, base + n, n, lane);
+    }
+    for (uint32_t o = lane; !done && o < nf; o += 32) {
+        bool keep; uint32_t cnt, xl, xu;
+        gs_fwd_rule(F, nf, o, B.smem, B.max_occ, keep, cnt, xl, xu);
+        if (keep && cnt) { seeds++; npos += cnt; }
+    }
+    for (uint32_t o = lane; !done && o < nr; o += 32) {
+        bool keep; uint32_t cnt, xl, xu;
+        gs_rev_rule(Rv, nr, o, B.smem, B.max_occ, keep, cnt, xl, xu);
+        if (keep && cnt) { seeds++; npos += cnt; }
+    }
+    for (int off = 16; off; off >>= 1) {
+        seeds += __shfl_xor_sync(0xffffffffu, seeds, off);
+        npos += __shfl_xor_sync(0xffffffffu, npos, off);
+    }
+    if (lane == 0) {
+        B.rd_nf[r] = nf;
+        B.rd_nr[r] = nr;
+        B.rd_nseeds[r] = seeds;
+        B.rd_npos[r] = npos;
+    }
+}
+
+/* 32 consecutive reads per warp: a lane compacts and counts its own read
+ * when it spans at most GS_LANE_SLOTS slots (few instructions a read, the
+ * warp's loads spread over 32 reads); the warp then takes its longer reads
+ * one at a time. */
 __global__ void __launch_bounds__(256) gs_finalize_count(GsBatch B)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    uint64_t so0 = 0, so1 = 0;
-    if (warp < B.n_reads) {
-        so0 = B.slot_off[warp];
-        so1 = B.slot_off[warp + 1];
-    }
-    for (uint32_t r = warp; r < B.n_reads; r += nwarps) {
-        const uint64_t base = so0, next = so1;
-        /* the next read's slot range, loaded while this one is compacted */
-        if (r + nwarps < B.n_reads) {
-            so0 = B.slot_off[r + nwarps];
-            so1 = B.slot_off[r + nwarps + 1];
-        }
-        if (next > B.slot_cap) {
-            /* a replayed pass whose input needs more slots than it was sized
-             * for: nothing of this read is there; the host re-sizes */
-            if (lane == 0) {
+    for (uint32_t r0 = warp * 32u; r0 < B.n_reads; r0 += nwarps * 32u) {
+        const uint32_t r = r0 + (uint32_t)lane;
+        uint64_t base = 0, next = 0;
+        bool longr = false;
+        if (r < B.n_reads) {
+            base = B.slot_off[r];
+            next = B.slot_off[r + 1];
+            if (next > B.slot_cap) {
+                /* a replayed pass whose input needs more slots than it was
+                 * sized for: nothing of this read is there; the host
+                 * re-sizes */
                 B.rd_nf[r] = 0;
                 B.rd_nr[r] = 0;
                 B.rd_nseeds[r] = 0;
                 B.rd_npos[r] = 0;
                 atomicOr(B.queue + 1, GS_FLAG_OVERFLOW);
+            } else if (next - base > GS_LANE_SLOTS) {
+                longr = true;
+            } else {
+                const uint32_t n = (uint32_t)((next - base) >> 1);
+                uint64_t seeds = 0, npos = 0;
+                const uint32_t nf = gs_lane_compact(B.slots, B.recmask, base, n, true, B.smem,
+                                                    B.max_occ, seeds, npos);
+                const uint32_t nr = gs_lane_compact(B.slots, B.recmask, base + n, n, false,
+                                                    B.smem, B.max_occ, seeds, npos);
+                B.rd_nf[r] = nf;
+                B.rd_nr[r] = nr;
+                B.rd_nseeds[r] = seeds;
+                B.rd_npos[r] = npos;
             }
-            continue;
         }
-        uint32_t n = (uint32_t)((next - base) >> 1);
-        GsRec *F = B.slots + base;
-        GsRec *Rv = F + n;
-        uint32_t nf, nr;
-        uint64_t seeds = 0, npos = 0;
-        bool done = false;
-        if (2u * n + 31u <= 1024u) {
-            GsRec mine;
-            gs_warp_compact_both(B.slots, B.recmask, base, n, lane, nf, nr, mine);
-            if (nf + nr <= 32u) {
-                /* lane j holds record j of [forward | reverse]: the rules'
-                 * neighbours are lanes j+1 (forward) and j-1 (reverse) */
-                GsRec up, dn;
-                up.x = __shfl_down_sync(0xffffffffu, mine.x, 1);
-                up.y = __shfl_down_sync(0xffffffffu, mine.y, 1);
-                up.l = __shfl_down_sync(0xffffffffu, mine.l, 1);
-                up.u = __shfl_down_sync(0xffffffffu, mine.u, 1);
-                dn.x = __shfl_up_sync(0xffffffffu, mine.x, 1);
-                dn.y = __shfl_up_sync(0xffffffffu, mine.y, 1);
-                dn.l = __shfl_up_sync(0xffffffffu, mine.l, 1);
-                dn.u = __shfl_up_sync(0xffffffffu, mine.u, 1);
-                const uint32_t j = (uint32_t)lane;
-                bool keep = false;
-                uint32_t cnt = 0, xl, xu;
-                if (j < nf)
-                    gs_fwd_rule_v(mine, up, j + 1 < nf, B.smem, B.max_occ, keep, cnt, xl, xu);
-                else if (j < nf + nr)
-                    gs_rev_rule_v(mine, dn, j > nf, B.smem, B.max_occ, keep, cnt, xl, xu);
-                if (keep && cnt) {
-                    seeds = 1;
-                    npos = cnt;
-                }
-                done = true;
-            }
-        } else {
-            nf = gs_warp_compact(B.slots, B.recmask, base, n, lane);
-            nr = gs_warp_compact(B.slots, B.recmask, base + n, n, lane);
-        }
-        for (uint32_t o = lane; !done && o < nf; o += 32) {
-            bool keep; uint32_t cnt, xl, xu;
-            gs_fwd_rule(F, nf, o, B.smem, B.max_occ, keep, cnt, xl, xu);
-            if (keep && cnt) { seeds++; npos += cnt; }
-        }
-        for (uint32_t o = lane; !done && o < nr; o += 32) {
-            bool keep; uint32_t cnt, xl, xu;
-            gs_rev_rule(Rv, nr, o, B.smem, B.max_occ, keep, cnt, xl, xu);
-            if (keep && cnt) { seeds++; npos += cnt; }
-        }
-        for (int off = 16; off; off >>= 1) {
-            seeds += __shfl_xor_sync(0xffffffffu, seeds, off);
-            npos += __shfl_xor_sync(0xffffffffu, npos, off);
-        }
-        if (lane == 0) {
-            B.rd_nf[r] = nf;
-            B.rd_nr[r] = nr;
-            B.rd_nseeds[r] = seeds;
-            B.rd_npos[r] = npos;
+        uint32_t lm = __ballot_sync(0xffffffffu, longr);
+        while (lm) {
+            const int src = __ffs(lm) - 1;
+            lm &= lm - 1u;
+            const uint64_t b0 = __shfl_sync(0xffffffffu, base, src);
+            const uint64_t b1 = __shfl_sync(0xffffffffu, next, src);
+            gs_finalize_read_warp(B, r0 + (uint32_t)src, b0, b1, lane);
         }
     }
 }
@@ -496,7 +575,7 @@ int gs_launch_finalize_count(const GsDevIndex &I, GsBatch &B, cudaStream_t st)
 {
     (void)I;
     if (B.n_reads == 0) return GS_OK;
-    uint32_t grid = (B.n_reads + 7) / 8;
+    uint32_t grid = (B.n_reads + 255) / 256;
     if (grid > 152u * 16u) grid = 152u * 16u;
     gs_finalize_count<<<grid, 256, 0, st>>>(B);
     GS_CUDA(cudaGetLastError());
