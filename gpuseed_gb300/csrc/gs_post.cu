@@ -404,19 +404,33 @@ __global__ void __launch_bounds__(128) gs_finalize_emit(GsBatch B, uint64_t *see
     uint64_t s = B.seed_off[r];
     uint64_t p = B.pos_off[r];
     uint32_t a = 0, b = 0;
+    /* each record loaded once: the forward list's current and next, the
+     * reverse list's current and previous */
+    GsRec none;
+    none.x = none.y = 0;
+    none.l = 1u;
+    none.u = 0u;
+    GsRec fc = nf ? F[0] : none, fn = nf > 1 ? F[1] : none;
+    GsRec rc = nr ? Rv[0] : none, rp = none;
     while (a < nf || b < nr) {
         bool take_f;
         if (a >= nf) take_f = false;
         else if (b >= nr) take_f = true;
-        else take_f = ((uint32_t)F[a].x & 0x7fffffffu) <= ((uint32_t)Rv[b].x & 0x7fffffffu);
+        else take_f = ((uint32_t)fc.x & 0x7fffffffu) <= ((uint32_t)rc.x & 0x7fffffffu);
         bool keep; uint32_t cnt, xl, xu;
         GsRec R;
         if (take_f) {
-            gs_fwd_rule(F, nf, a, B.smem, B.max_occ, keep, cnt, xl, xu);
-            R = F[a++];
+            gs_fwd_rule_v(fc, fn, a + 1 < nf, B.smem, B.max_occ, keep, cnt, xl, xu);
+            R = fc;
+            a++;
+            fc = fn;
+            fn = a + 1 < nf ? F[a + 1] : none;
         } else {
-            gs_rev_rule(Rv, nr, b, B.smem, B.max_occ, keep, cnt, xl, xu);
-            R = Rv[b++];
+            gs_rev_rule_v(rc, rp, b > 0, B.smem, B.max_occ, keep, cnt, xl, xu);
+            R = rc;
+            b++;
+            rp = rc;
+            rc = b < nr ? Rv[b] : none;
         }
         if (keep && cnt) {
             if (s < B.seed_cap) {
