@@ -125,7 +125,9 @@ __device__ __forceinline__ int gs_step(const GsDevIndex &I, uint32_t &l, uint32_
 
 /* The part of a block one occurrence query with base c reads: the count
  * of c before the block and the four bit-slice words (a 4-byte and a
- * 16-byte load of the same 32-byte sector). */
+ * 16-byte load of the same 32-byte sector).  Their L2 fills are 64 bytes
+ * (the block and its neighbour), not 128: config-3 search 101.25 -> 100.9
+ * ms (256-byte fills: 101.5). */
 struct GsHalf {
     uint32_t cnt, h0, h1, l0, l1;
 };
@@ -134,8 +136,8 @@ __device__ __forceinline__ GsHalf gs_load_half(const uint32_t *occ, uint32_t blk
 {
     GsHalf h;
     const uint32_t *p = occ + (size_t)blk * GS_BLOCK_WORDS;
-    asm("ld.global.nc.u32 %0, [%1];" : "=r"(h.cnt) : "l"(p + c));
-    asm("ld.global.nc.v4.u32 {%0,%1,%2,%3}, [%4];"
+    asm("ld.global.nc.L2::64B.u32 %0, [%1];" : "=r"(h.cnt) : "l"(p + c));
+    asm("ld.global.nc.L2::64B.v4.u32 {%0,%1,%2,%3}, [%4];"
         : "=r"(h.h0), "=r"(h.h1), "=r"(h.l0), "=r"(h.l1)
         : "l"(p + 4));
     return h;
