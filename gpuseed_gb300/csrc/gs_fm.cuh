@@ -22,11 +22,19 @@ struct GsBlk {
     uint32_t w[8];
 };
 
+/* one random read-only word with a 64-byte L2 fill (the default fills 128) */
+__device__ __forceinline__ uint32_t gs_ld64(const uint32_t *p)
+{
+    uint32_t v;
+    asm("ld.global.nc.L2::64B.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+
 __device__ __forceinline__ GsBlk gs_load_block(const uint32_t *occ, uint32_t blk)
 {
     GsBlk b;
     const uint32_t *p = occ + (size_t)blk * GS_BLOCK_WORDS;
-    asm("ld.global.nc.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+    asm("ld.global.nc.L2::64B.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
         : "=r"(b.w[0]), "=r"(b.w[1]), "=r"(b.w[2]), "=r"(b.w[3]), "=r"(b.w[4]), "=r"(b.w[5]),
           "=r"(b.w[6]), "=r"(b.w[7])
         : "l"(p));

@@ -553,7 +553,7 @@ __global__ void __launch_bounds__(256) gs_locate(GsDevIndex I, const gs_seed_rec
             const uint32_t cap = I.seq_len + 2u;
             bool bad = false;
             if (I.saf) {
-                uint32_t v = __ldg(&I.saf[row]);
+                uint32_t v = gs_ld64(&I.saf[row]);
                 if (lf_mode == GS_LF_GPUSEED && v - I.quirk_lo < I.quirk_n) v -= I.quirk_lo;
                 out[j] = v;
             }

@@ -819,7 +819,7 @@ __device__ __forceinline__ bool gs_text_round(const GsDevIndex &I, const unsigne
     const uint32_t ph = (jl >> 26) & 3u;
     (void)wb;
     if (ph == 0) {
-        ju = __ldg(&I.saf[l]);
+        ju = gs_ld64(&I.saf[l]);
         jl = GS_TEXT_MARK | (1u << 26);
         return true;
     }
@@ -835,7 +835,7 @@ __device__ __forceinline__ bool gs_text_round(const GsDevIndex &I, const unsigne
             uint32_t wt;
             if (q >= 16) {
                 const uint32_t b = q - 16u;
-                wt = __funnelshift_r(__ldg(&I.text[b >> 4]), __ldg(&I.text[(b >> 4) + 1]),
+                wt = __funnelshift_r(gs_ld64(&I.text[b >> 4]), gs_ld64(&I.text[(b >> 4) + 1]),
                                      (b & 15u) << 1);
             } else {
                 wt = __ldg(&I.text[0]) << ((16u - q) << 1);
@@ -870,8 +870,8 @@ __device__ __forceinline__ bool gs_text_round(const GsDevIndex &I, const unsigne
         uint32_t qp = (qs + GS_ISA_STEP - 1u) & ~(GS_ISA_STEP - 1u);
         uint32_t row = 0;
         if (qp > I.seq_len) qp = I.seq_len;
-        else row = __ldg(&I.isa[qp / GS_ISA_STEP]);
-        const uint32_t w = __funnelshift_r(__ldg(&I.text[qs >> 4]), __ldg(&I.text[(qs >> 4) + 1]),
+        else row = gs_ld64(&I.isa[qp / GS_ISA_STEP]);
+        const uint32_t w = __funnelshift_r(gs_ld64(&I.text[qs >> 4]), gs_ld64(&I.text[(qs >> 4) + 1]),
                                            (qs & 15u) << 1);
         l = u = row;
         const uint32_t d = qp - qs;
