@@ -692,7 +692,7 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
                 "peak_source": f"{peak_src} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
-                "kernel": "gs_search_start + gs_search_walk + gs_search_text (one search pass)",
+                "kernel": "gs_search_start + gs_search_walk + gs_search_text + gs_search_leftover (one search pass)",
                 "algorithmic_bytes_per_launch": canon_bytes if canon_bytes else own_bytes,
                 "algorithmic_count": ("canonical containment-stopped walk from the 13-mer table "
                                       "(oracle sample, scaled by candidates)") if canon_bytes else
