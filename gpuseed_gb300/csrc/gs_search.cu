@@ -1226,9 +1226,9 @@ __device__ __forceinline__ void gs_start_pair_item(const GsDevIndex &I, const Gs
     }
 }
 
-template <int NSTOP, int COUNT, bool PAIRED>
 /* 5 CTAs of 256 per SM (48 registers, no spills): more lookups in flight
  * than 4 or 3 (config-3 search 101.1 / 101.8 / 104.5 ms) */
+template <int NSTOP, int COUNT, bool PAIRED>
 __global__ void __launch_bounds__(256, 5) gs_search_start(GsDevIndex I, GsBatch B, int queue_chunk)
 {
     const int lane = threadIdx.x & 31;
