@@ -329,10 +329,11 @@ def test_longer_start_table(small, kx):
         # leftover pass, which walks them without J
         for slots in (1, -1):
             for n_mode in (0, 1):
-                gres = small["ctx"].seed(seqs, offs, lens, k=kx + 3, smem=True, n_mode=n_mode,
-                                         kernel=0, walker_slots=slots)
-                ob = small["oidx"].seed(seqs, offs, lens, k=kx + 3, smem=True, n_mode=n_mode)
-                assert_same(gres, ob, len(reads), f"kx={kx} slots={slots} n={n_mode}")
+                for smem in (False, True):
+                    gres = small["ctx"].seed(seqs, offs, lens, k=kx + 3, smem=smem, n_mode=n_mode,
+                                             kernel=0, walker_slots=slots)
+                    ob = small["oidx"].seed(seqs, offs, lens, k=kx + 3, smem=smem, n_mode=n_mode)
+                    assert_same(gres, ob, len(reads), f"kx={kx} slots={slots} n={n_mode} smem={smem}")
     finally:
         small["gidx"].set_kmer_len(13)
 
@@ -355,7 +356,7 @@ def test_handoff_settings(small, lanes, steps):
 @pytest.mark.parametrize("slots", [-1, 1, 0, 496])
 def test_walker_buffer(small, slots):
     """The batched search gives the same seeds whether its survivors are walked
-    by the walk pass, by the start pass (no buffer), or split between them
+    by the walk pass, by the leftover pass (no buffer), or split between them
     (a buffer that overflows)."""
     reads = sample_reads(small["codes"], 400, seed=80 + slots, lengths=(30, 100, 150, 300, 700),
                          err=0.02, n_rate=0.3)
